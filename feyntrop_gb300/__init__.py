@@ -1,0 +1,240 @@
+"""feyntrop_gb300: feyntrop's tropical sampling + integrand evaluation loop on GB300.
+
+Python side of the C ABI in include/feyntrop_gb300.h (ctypes, no torch types).
+The sampling runs only on the GPU: without the native library or without a
+CUDA device every entry point raises instead of falling back to anything else.
+
+    from feyntrop_gb300 import Plan, run_json
+    plan = Plan(input_dict)                  # the reference's JSON schema
+    out = plan.integrate(N=10**7, seed=0)    # {"integral": [[[re, dre], [im, dim]], ...], ...}
+    out = run_json(input_dict)               # the CLI contract, in process
+
+py_feyntrop (the reference's Python front end) is mirrored in
+feyntrop_gb300.py_feyntrop.
+"""
+import ctypes
+import json
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfeyntrop_gb300.so")
+CLI_PATH = os.path.join(HERE, "_build", "feyntrop")
+
+FT_OK = 0
+FT_ERR_INVALID_ARGUMENT = 1
+FT_ERR_DOMAIN = 2
+FT_ERR_RUNTIME = 3
+FT_ERR_CUDA = 4
+FT_ERR_NO_DEVICE = 5
+FP64 = 0
+MIXED = 1
+
+EXPORTED = ["ft_plan_create", "ft_plan_destroy", "ft_plan_get_info", "ft_plan_log_line", "ft_integrate",
+            "ft_integrate_batch", "ft_finalize_moments", "ft_sample_records", "ft_run_json", "ft_free",
+            "ft_precompile", "ft_last_error", "ft_version"]
+
+
+class FeyntropError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(message)
+        self.code = code
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("num_edges", ctypes.c_int32), ("edges", ctypes.c_void_p), ("nu", ctypes.c_void_p),
+                ("num_vertices", ctypes.c_int32), ("scalarproducts", ctypes.c_void_p),
+                ("masses_sqr", ctypes.c_void_p), ("dimension", ctypes.c_double), ("num_eps_terms", ctypes.c_int32),
+                ("lambda_", ctypes.c_double)]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [("W", ctypes.c_double), ("IGtr", ctypes.c_double), ("loops", ctypes.c_int32),
+                ("euclidean", ctypes.c_int32), ("pseudo_euclidean", ctypes.c_int32), ("generic", ctypes.c_int32),
+                ("gp_property", ctypes.c_int32), ("deformed", ctypes.c_int32), ("lambda_used", ctypes.c_double),
+                ("seconds_preprocessing", ctypes.c_double), ("table_bytes", ctypes.c_uint64),
+                ("num_log_lines", ctypes.c_int32)]
+
+
+class RunOptions(ctypes.Structure):
+    _fields_ = [("num_samples", ctypes.c_uint64), ("seed", ctypes.c_uint64), ("first_sample", ctypes.c_uint64),
+                ("precision", ctypes.c_int32), ("stream", ctypes.c_void_p)]
+
+
+class Moments(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_double), ("s1_hi", ctypes.c_double), ("s1_lo", ctypes.c_double),
+                ("s2_hi", ctypes.c_double), ("s2_lo", ctypes.c_double)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("num_eps_terms", ctypes.c_int32), ("re_avg", ctypes.c_void_p), ("re_acc", ctypes.c_void_p),
+                ("im_avg", ctypes.c_void_p), ("im_acc", ctypes.c_void_p), ("moments", ctypes.c_void_p),
+                ("kept", ctypes.c_uint64), ("dropped", ctypes.c_uint64), ("fp64_fallback", ctypes.c_uint64),
+                ("exact_steps", ctypes.c_uint64), ("robust", ctypes.c_uint64), ("kernel_ms", ctypes.c_double),
+                ("seconds_sampling", ctypes.c_double), ("kernel_launches", ctypes.c_int32)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def lib():
+    """The native library; raises if it has not been built (no fallback path exists)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError("feyntrop_gb300 native library missing (%s): build it with "
+                                  "`python -m feyntrop_gb300.build`" % LIB_PATH)
+            L = ctypes.CDLL(LIB_PATH)
+            L.ft_last_error.restype = ctypes.c_char_p
+            L.ft_version.restype = ctypes.c_char_p
+            L.ft_plan_log_line.restype = ctypes.c_char_p
+            L.ft_plan_create.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(ctypes.c_void_p)]
+            L.ft_plan_destroy.argtypes = [ctypes.c_void_p]
+            L.ft_plan_get_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(PlanInfo)]
+            L.ft_plan_log_line.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+            L.ft_integrate.argtypes = [ctypes.c_void_p, ctypes.POINTER(RunOptions), ctypes.POINTER(Result)]
+            L.ft_integrate_batch.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+            L.ft_finalize_moments.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                              ctypes.POINTER(Result)]
+            L.ft_sample_records.argtypes = [ctypes.c_void_p, ctypes.POINTER(RunOptions)] + [ctypes.c_void_p] * 4
+            L.ft_run_json.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_void_p),
+                                      ctypes.POINTER(ctypes.c_void_p)]
+            L.ft_free.argtypes = [ctypes.c_void_p]
+            L.ft_precompile.argtypes = [ctypes.POINTER(Problem), ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+            L.ft_subgraph_table.argtypes = [ctypes.POINTER(Problem)] + [ctypes.c_void_p] * 4 + [
+                ctypes.POINTER(PlanInfo)]
+            _lib = L
+        return _lib
+
+
+def _check(rc):
+    if rc != FT_OK:
+        raise FeyntropError(rc, lib().ft_last_error().decode(errors="replace"))
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class _ProblemArrays:
+    """Keeps the numpy arrays behind an ft_problem alive."""
+
+    def __init__(self, inp):
+        if isinstance(inp, str):
+            inp = json.loads(inp)
+        self.inp = inp
+        self.edges = np.ascontiguousarray([[int(e[0][0]), int(e[0][1])] for e in inp["graph"]],
+                                          dtype=np.int32).reshape(-1)
+        self.nu = np.ascontiguousarray([float(e[1]) for e in inp["graph"]], dtype=np.float64)
+        self.P = np.ascontiguousarray(np.array(inp["scalarproducts"], dtype=np.float64).reshape(-1))
+        self.m2 = np.ascontiguousarray(inp["masses_sqr"], dtype=np.float64)
+        self.V = int(self.edges.max()) + 1 if len(self.edges) else 0
+        self.E = len(self.nu)
+        self.K = int(inp["num_eps_terms"])
+        self.struct = Problem(self.E, _ptr(self.edges).value, _ptr(self.nu).value, self.V, _ptr(self.P).value,
+                              _ptr(self.m2).value, float(inp["dimension"]), self.K, float(inp["lambda"]))
+
+
+def subgraph_table(inp):
+    """Host preprocessing only: (Jr, r, mm, loops, info) of the J(gamma) table."""
+    a = _ProblemArrays(inp)
+    n = 1 << a.E
+    Jr, r = np.zeros(n), np.zeros(n)
+    mm, L = np.zeros(n, np.uint8), np.zeros(n, np.uint8)
+    info = PlanInfo()
+    _check(lib().ft_subgraph_table(ctypes.byref(a.struct), _ptr(Jr), _ptr(r), _ptr(mm), _ptr(L), ctypes.byref(info)))
+    return Jr, r, mm, L, {f: getattr(info, f) for f, _ in PlanInfo._fields_}
+
+
+def precompile(inp, precision=MIXED):
+    """Compile the kernels of this input's topology into the cache; returns seconds."""
+    a = _ProblemArrays(inp)
+    s = ctypes.c_double()
+    _check(lib().ft_precompile(ctypes.byref(a.struct), precision, ctypes.byref(s)))
+    return s.value
+
+
+class Plan:
+    """One integral on the GPU (host preprocessing + device tables)."""
+
+    def __init__(self, inp):
+        self.arrays = _ProblemArrays(inp)
+        self.E, self.V, self.K = self.arrays.E, self.arrays.V, self.arrays.K
+        h = ctypes.c_void_p()
+        _check(lib().ft_plan_create(ctypes.byref(self.arrays.struct), ctypes.byref(h)))
+        self.h = h
+        info = PlanInfo()
+        _check(lib().ft_plan_get_info(self.h, ctypes.byref(info)))
+        self.info = {f: getattr(info, f) for f, _ in PlanInfo._fields_}
+        self.log = [lib().ft_plan_log_line(self.h, i).decode() for i in range(info.num_log_lines)]
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ft_plan_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def integrate(self, N, seed=0, precision=FP64, first_sample=0, stream=None):
+        K = self.K
+        arr = np.zeros((4, K))
+        mom = (Moments * (2 * K))()
+        res = Result(K, _ptr(arr[0]).value, _ptr(arr[1]).value, _ptr(arr[2]).value, _ptr(arr[3]).value,
+                     ctypes.cast(mom, ctypes.c_void_p).value)
+        opts = RunOptions(int(N), int(seed), int(first_sample), int(precision), stream)
+        _check(lib().ft_integrate(self.h, ctypes.byref(opts), ctypes.byref(res)))
+        return {
+            "integral": [[[arr[0, j], arr[1, j]], [arr[2, j], arr[3, j]]] for j in range(K)],
+            "IGtr": self.info["IGtr"],
+            "moments": [[m.n, m.s1_hi, m.s1_lo, m.s2_hi, m.s2_lo] for m in mom],
+            "kept": res.kept, "dropped": res.dropped, "fp64_fallback": res.fp64_fallback,
+            "exact_steps": res.exact_steps, "robust": res.robust, "kernel_ms": res.kernel_ms,
+            "seconds_sampling": res.seconds_sampling, "kernel_launches": res.kernel_launches,
+        }
+
+    def records(self, count, seed=0, first_sample=0, precision=FP64):
+        """Per-sample records of samples first_sample .. first_sample+count-1."""
+        E, K = self.E, self.K
+        order = np.zeros((count, E), np.uint8)
+        X = np.zeros((count, E))
+        R = np.zeros((count, K, 2))
+        flags = np.zeros(count, np.uint8)
+        opts = RunOptions(int(count), int(seed), int(first_sample), int(precision), None)
+        _check(lib().ft_sample_records(self.h, ctypes.byref(opts), _ptr(order), _ptr(X), _ptr(R), _ptr(flags)))
+        return {"order": order.astype(np.int32), "X": X, "R": R[..., 0] + 1j * R[..., 1], "flags": flags}
+
+
+def finalize_moments(moments, K, real_only):
+    """avg/acc from merged moments (list of 2K [n, s1_hi, s1_lo, s2_hi, s2_lo])."""
+    m = (Moments * (2 * K))(*[Moments(*x) for x in moments])
+    arr = np.zeros((4, K))
+    res = Result(K, _ptr(arr[0]).value, _ptr(arr[1]).value, _ptr(arr[2]).value, _ptr(arr[3]).value, None)
+    _check(lib().ft_finalize_moments(ctypes.cast(m, ctypes.c_void_p), K, 1 if real_only else 0, ctypes.byref(res)))
+    return [[[arr[0, j], arr[1, j]], [arr[2, j], arr[3, j]]] for j in range(K)]
+
+
+def run_json(inp, with_log=False):
+    """The reference's CLI contract in process: input (dict or JSON text) -> output dict."""
+    text = inp if isinstance(inp, str) else json.dumps(inp)
+    out = ctypes.c_void_p()
+    log = ctypes.c_void_p()
+    L = lib()
+    rc = L.ft_run_json(text.encode(), ctypes.byref(out), ctypes.byref(log))
+    log_text = ctypes.string_at(log.value).decode() if log.value else ""
+    if log.value:
+        L.ft_free(log)
+    if rc != FT_OK:
+        if out.value:
+            L.ft_free(out)
+        raise FeyntropError(rc, log_text.strip())
+    res = json.loads(ctypes.string_at(out.value).decode().replace("NaN", "null"))
+    L.ft_free(out)
+    return (res, log_text) if with_log else res

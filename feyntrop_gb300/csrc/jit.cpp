@@ -1,0 +1,227 @@
+#include "jit.hpp"
+
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+#include <nvrtc.h>
+#include <sys/stat.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+
+extern const char* ft_sample_body_source;   // generated at build time from kernels/sample_body.cuh
+
+namespace ft {
+
+static const char* kArch = "--gpu-architecture=sm_103a";
+
+unsigned table_smem_bytes(const kernel_key& k)
+{
+    if (k.table_global) return 0;
+    const unsigned entries = 1u << k.E;
+    const unsigned b = k.prec == 0 ? 25u * entries : 13u * entries;
+    return (b + 15u) & ~15u;
+}
+
+std::string kernel_source(const kernel_key& k)
+{
+    std::ostringstream s;
+    s << "// generated: one topology of the tropical sampling kernel\n";
+    s << "#define FT_E " << k.E << "\n#define FT_V " << k.V << "\n#define FT_K " << k.K << "\n";
+    s << "#define FT_LOOPS " << k.loops << "\n#define FT_RANK " << k.rank << "\n";
+    s << "#define FT_PREC " << k.prec << "\n#define FT_MODE " << k.mode << "\n";
+    s << "#define FT_ONLY_PSI " << k.only_psi << "\n#define FT_RECORD " << k.record << "\n";
+    s << "#define FT_BLOCK " << k.block << "\n#define FT_TABLE_GLOBAL " << k.table_global << "\n";
+    s << "__device__ constexpr int FT_EK[" << k.E << "] = {";
+    for (int e = 0; e < k.E; e++) s << (e ? "," : "") << k.ek[e];
+    s << "};\n__device__ constexpr int FT_EL[" << k.E << "] = {";
+    for (int e = 0; e < k.E; e++) s << (e ? "," : "") << k.el[e];
+    s << "};\n";
+    s << ft_sample_body_source;
+    return s.str();
+}
+
+static uint64_t fnv1a(const std::string& s)
+{
+    uint64_t h = 1469598103934665603ULL;
+    for (unsigned char c : s) {
+        h ^= c;
+        h *= 1099511628211ULL;
+    }
+    return h;
+}
+
+static std::string cache_dir()
+{
+    if (const char* env = std::getenv("FEYNTROP_GB300_CACHE")) return env;
+    Dl_info info;
+    if (dladdr((void*)&cache_dir, &info) && info.dli_fname) {
+        std::string p = info.dli_fname;
+        size_t slash = p.rfind('/');
+        if (slash != std::string::npos) return p.substr(0, slash) + "/../_jit_cache";
+    }
+    return "_jit_cache";
+}
+
+static std::vector<std::string> options()
+{
+    return {kArch, "--std=c++17", "-lineinfo", "--extra-device-vectorization"};
+}
+
+static std::string compile(const std::string& src, std::string* log_out)
+{
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "ft_sample.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS)
+        throw std::runtime_error("nvrtcCreateProgram failed");
+    std::vector<std::string> opts = options();
+    std::vector<const char*> o;
+    for (auto& x : opts) o.push_back(x.c_str());
+    if (std::getenv("FEYNTROP_GB300_PTXAS_VERBOSE")) o.push_back("--ptxas-options=-v");
+    nvrtcResult rc = nvrtcCompileProgram(prog, (int)o.size(), o.data());
+    size_t logn = 0;
+    nvrtcGetProgramLogSize(prog, &logn);
+    std::string log(logn, '\0');
+    if (logn) nvrtcGetProgramLog(prog, &log[0]);
+    if (log_out) *log_out = log;
+    if (rc != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        throw std::runtime_error("kernel compilation failed:\n" + log);
+    }
+    if (std::getenv("FEYNTROP_GB300_PTXAS_VERBOSE")) std::fprintf(stderr, "%s\n", log.c_str());
+    size_t n = 0;
+    nvrtcGetCUBINSize(prog, &n);
+    std::string cubin(n, '\0');
+    nvrtcGetCUBIN(prog, &cubin[0]);
+    nvrtcDestroyProgram(&prog);
+    return cubin;
+}
+
+static std::string cubin_for(const kernel_key& key, double* seconds)
+{
+    const std::string src = kernel_source(key);
+    std::string tag = src;
+    for (auto& o : options()) tag += o;
+    int major = 0, minor = 0;
+    nvrtcVersion(&major, &minor);
+    tag += std::to_string(major) + "." + std::to_string(minor);
+    char name[64];
+    std::snprintf(name, sizeof name, "%016llx.cubin", (unsigned long long)fnv1a(tag));
+    const std::string dir = cache_dir();
+    const std::string path = dir + "/" + name;
+    {
+        std::ifstream f(path, std::ios::binary);
+        if (f) {
+            std::stringstream b;
+            b << f.rdbuf();
+            std::string s = b.str();
+            if (!s.empty()) {
+                *seconds = 0;
+                return s;
+            }
+        }
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    std::string cubin = compile(src, nullptr);
+    *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    mkdir(dir.c_str(), 0755);
+    const std::string tmp = path + ".tmp" + std::to_string((unsigned long long)fnv1a(std::to_string((long)&tag)));
+    {
+        std::ofstream f(tmp, std::ios::binary);
+        f.write(cubin.data(), (std::streamsize)cubin.size());
+    }
+    std::rename(tmp.c_str(), path.c_str());
+    return cubin;
+}
+
+size_t compile_only(const kernel_key& key, std::string* log) { return compile(kernel_source(key), log).size(); }
+
+void precompile(const kernel_key& key)
+{
+    double s = 0;
+    cubin_for(key, &s);
+}
+
+// Driver entry points are fetched through the runtime (no link-time dependency on
+// the driver library, so the library also loads on machines without a GPU).
+driver_api& drv()
+{
+    static driver_api d;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        auto get = [](const char* name, void** fn) {
+            cudaDriverEntryPointQueryResult q;
+            if (cudaGetDriverEntryPointByVersion(name, fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+                q != cudaDriverEntryPointSuccess || !*fn)
+                throw std::runtime_error(std::string("driver entry point unavailable: ") + name);
+        };
+        get("cuModuleLoadData", (void**)&d.ModuleLoadData);
+        get("cuModuleGetFunction", (void**)&d.ModuleGetFunction);
+        get("cuFuncSetAttribute", (void**)&d.FuncSetAttribute);
+        get("cuFuncGetAttribute", (void**)&d.FuncGetAttribute);
+        get("cuOccupancyMaxActiveBlocksPerMultiprocessor", (void**)&d.OccupancyMaxActiveBlocksPerMultiprocessor);
+        get("cuLaunchKernel", (void**)&d.LaunchKernel);
+        get("cuGetErrorString", (void**)&d.GetErrorString);
+    });
+    return d;
+}
+
+void check(CUresult r, const char* what)
+{
+    if (r != CUDA_SUCCESS) {
+        const char* msg = nullptr;
+        drv().GetErrorString(r, &msg);
+        throw std::runtime_error(std::string(what) + ": " + (msg ? msg : "unknown driver error"));
+    }
+}
+
+static std::string key_string(const kernel_key& k)
+{
+    std::ostringstream s;
+    s << k.E << "," << k.V << "," << k.K << "," << k.loops << "," << k.rank << "," << k.prec << "," << k.mode << ","
+      << k.only_psi << "," << k.record << "," << k.block << "," << k.table_global;
+    for (int e = 0; e < k.E; e++) s << ";" << k.ek[e] << "-" << k.el[e];
+    return s.str();
+}
+
+const kernel_set& get_kernels(const kernel_key& key)
+{
+    static std::mutex mu;
+    static std::map<std::pair<int, std::string>, kernel_set> loaded;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) throw std::runtime_error("no CUDA device");
+    std::lock_guard<std::mutex> lock(mu);
+    auto k = std::make_pair(dev, key_string(key));
+    auto it = loaded.find(k);
+    if (it != loaded.end()) return it->second;
+
+    cudaFree(0);   // make the runtime's primary context current for the driver calls
+    kernel_set ks;
+    ks.block = key.block;
+    const std::string cubin = cubin_for(key, &ks.compile_seconds);
+    check(drv().ModuleLoadData(&ks.module, cubin.data()), "cuModuleLoadData");
+    check(drv().ModuleGetFunction(&ks.sample, ks.module, "ft_sample"), "cuModuleGetFunction(ft_sample)");
+    if (key.prec == 0) check(drv().ModuleGetFunction(&ks.queue, ks.module, "ft_sample_queue"), "cuModuleGetFunction(queue)");
+    ks.smem = table_smem_bytes(key);
+    CUfunction fs[2] = {ks.sample, ks.queue};
+    for (CUfunction f : fs) {
+        if (!f) continue;
+        check(drv().FuncSetAttribute(f, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, (int)ks.smem),
+              "cuFuncSetAttribute(smem)");
+    }
+    check(drv().FuncGetAttribute(&ks.regs, CU_FUNC_ATTRIBUTE_NUM_REGS, ks.sample), "cuFuncGetAttribute");
+    check(drv().FuncGetAttribute(&ks.local_bytes, CU_FUNC_ATTRIBUTE_LOCAL_SIZE_BYTES, ks.sample), "cuFuncGetAttribute");
+    check(drv().OccupancyMaxActiveBlocksPerMultiprocessor(&ks.blocks_per_sm, ks.sample, ks.block, ks.smem),
+          "cuOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (ks.queue)
+        check(drv().OccupancyMaxActiveBlocksPerMultiprocessor(&ks.queue_blocks_per_sm, ks.queue, ks.block, ks.smem),
+              "cuOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (ks.blocks_per_sm < 1) throw std::runtime_error("sampling kernel does not fit on an SM");
+    return loaded.emplace(k, ks).first->second;
+}
+
+}  // namespace ft

@@ -1,0 +1,1472 @@
+// Per-sample tropical Monte Carlo kernel body, compiled at run time for one graph
+// topology (the host prepends the constants below and compiles with NVRTC for
+// sm_103a, so every edge endpoint is a compile-time constant and all matrices live
+// in registers).
+//
+// Required definitions:
+//   FT_E, FT_V        edges, vertices            FT_K        eps orders
+//   FT_LOOPS          loop number                FT_RANK     rank of the reduced P
+//   FT_PREC           0: plain FP64, 1: mixed FP32 with FP64 sampling decisions
+//   FT_MODE           0: undeformed integrand (srcs/feynman_integral.hpp:218-276)
+//                     1: deformed integrand  (srcs/feynman_integral.hpp:278-362)
+//   FT_ONLY_PSI       1 when W = 0 and one eps order (only psi is needed)
+//   FT_RECORD         1: write per-sample records
+//   FT_BLOCK          threads per block
+//   FT_EK[], FT_EL[]  edge endpoints (FT_EK[e] > FT_EL[e])
+//
+// One thread owns one sample at a time and walks a contiguous block of samples of
+// the seed's single xoshiro256+ stream, so the samples are exactly those of the
+// reference run with one OpenMP thread (srcs/feynman_integral.hpp:144-164).
+//
+// Numerical design (the reference's algebra, restated for a GPU thread):
+//  * Sector draw (srcs/tropical_sampling.hpp:468-564): the cut scan compares running
+//    sums of Jr/r against u*Jr in FP64 in the reference's order, so the removal order
+//    is bit-identical.  The mixed form decides each comparison in FP32 with a
+//    rigorous error margin and repeats the scan in FP64 when a comparison falls
+//    inside the margin.  The mixed form keeps log X in a two-float sum.
+//  * The deleted vertex of the reduced Laplacian is always the last one.  Any choice
+//    gives the same psi, phi/psi and derivatives (matrix-tree theorem and momentum
+//    conservation); the reference's choice only affects rounding.
+//  * The real reduced Laplacian is eliminated in conductance form: pivots are sums
+//    of positive conductances and updates add positive products, so psi = det L *
+//    prod X has full relative accuracy whatever the spread of X.
+//  * phi/psi = -tr(L^-1 P~) with P~ = sum_r sigma_r q_r q_r^T (host eigen-split):
+//    each term is a forward substitution with the elimination multipliers.
+//  * Deformed branch: L^-1 from the positive factors, x-derivatives of phi/psi
+//    (srcs/laplacian.hpp:102-215), the complex Laplacian eliminated in the same
+//    conductance form with a pivot-growth check (samples failing it take a
+//    complete-pivoting LU, srcs/feynman_integral.hpp:305), and the Jacobian
+//    determinant as det(I + i*lambda' X^1/2 H X^1/2) (similar to
+//    I + i*lambda' H X, srcs/feynman_integral.hpp:312), whose real part is the
+//    identity, so symmetric elimination without pivoting is stable.
+
+#ifndef FT_E
+#error "topology constants missing"
+#endif
+
+typedef unsigned long long u64;
+typedef unsigned int u32;
+
+#define FT_N (FT_V - 1)
+#define FT_FULL ((1u << FT_E) - 1u)
+#define FT_NPAIR (FT_E * (FT_E - 1) / 2)
+
+// ------------------------------------------------------------------ parameter block
+// doubles: 0 D, 1 W, 2 IGtr, 3 def_ref, 4 1/(D/2*L+W), 5 Jr(full), 6 unused, 7 unused,
+// then m2[E], nu[E], sigma[RANK], q[RANK][N]
+#define P_D 0
+#define P_W 1
+#define P_IGTR 2
+#define P_DEF 3
+#define P_NORM 4
+#define P_JRFULL 5
+#define P_M2 8
+#define P_NU (8 + FT_E)
+#define P_SIG (8 + 2 * FT_E)
+#define P_Q (8 + 2 * FT_E + FT_RANK)
+#define P_SIZE (8 + 2 * FT_E + FT_RANK + FT_RANK * FT_N)
+// the same block as floats follows at prm + P_SIZE (mixed form reads only that)
+
+// ------------------------------------------------------------------ table layout
+// [w64 | Jr64 | rinv64 : 8 bytes each][meta : 1 byte][pad to 16][w32 | Jr32 | rinv32]
+#define T_ENTRIES (1u << FT_E)
+#define T_W64 0
+#define T_JR64 (8u * T_ENTRIES)
+#define T_RI64 (16u * T_ENTRIES)
+#define T_META (24u * T_ENTRIES)
+#define T_F32 ((25u * T_ENTRIES + 15u) & ~15u)
+#define T_W32 (T_F32)
+#define T_JR32 (T_F32 + 4u * T_ENTRIES)
+#define T_RI32 (T_F32 + 8u * T_ENTRIES)
+
+// ------------------------------------------------------------------ accumulator slots
+// per eps order j: [8j + 0..7] = re S1 (hi, lo), re S2 (hi, lo), im S1 (hi, lo), im S2 (hi, lo)
+// then [8K] kept, [8K+1] dropped, [8K+2] queued, [8K+3] exact sampling steps,
+// [8K+4] robust factorisations
+#define ACC_KEPT (8 * FT_K)
+#define ACC_DROPPED (8 * FT_K + 1)
+#define ACC_QUEUED (8 * FT_K + 2)
+#define ACC_EXACT (8 * FT_K + 3)
+#define ACC_ROBUST (8 * FT_K + 4)
+#define ACC_SLOTS (8 * FT_K + 8)
+
+// record flags
+#define REC_DROPPED 1
+#define REC_QUEUED 2
+#define REC_EXACT 4
+#define REC_ROBUST 8
+
+// ------------------------------------------------------------------ small helpers
+static __device__ __forceinline__ u64 rotl64(u64 x, int k) { return (x << k) | (x >> (64 - k)); }
+
+struct xo {
+    u64 a, b, c, d;
+    __device__ __forceinline__ u64 next()
+    {
+        const u64 out = a + d;
+        const u64 t = b << 17;
+        c ^= a;
+        d ^= b;
+        b ^= c;
+        a ^= d;
+        c ^= t;
+        d = rotl64(d, 45);
+        return out;
+    }
+};
+
+static __device__ __forceinline__ double u01(u64 x) { return (double)(x >> 11) * 0x1.0p-53; }
+
+template <class T>
+struct cx {
+    T re, im;
+};
+template <class T>
+static __device__ __forceinline__ cx<T> cmk(T r, T i)
+{
+    cx<T> z;
+    z.re = r;
+    z.im = i;
+    return z;
+}
+template <class T>
+static __device__ __forceinline__ cx<T> operator+(cx<T> a, cx<T> b) { return cmk(a.re + b.re, a.im + b.im); }
+template <class T>
+static __device__ __forceinline__ cx<T> operator-(cx<T> a, cx<T> b) { return cmk(a.re - b.re, a.im - b.im); }
+template <class T>
+static __device__ __forceinline__ cx<T> operator*(cx<T> a, cx<T> b)
+{
+    return cmk(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re);
+}
+template <class T>
+static __device__ __forceinline__ cx<T> operator*(T s, cx<T> a) { return cmk(s * a.re, s * a.im); }
+template <class T>
+static __device__ __forceinline__ cx<T> crecip(cx<T> z)
+{
+    // scaled so that |z|^2 cannot overflow in single precision
+    T s = fmax(fabs(z.re), fabs(z.im));
+    T r = z.re / s, i = z.im / s;
+    T d = s * (r * r + i * i);
+    return cmk(r / d, -i / d);
+}
+static __device__ __forceinline__ double cabs_(cx<double> z) { return hypot(z.re, z.im); }
+static __device__ __forceinline__ float cabs_(cx<float> z) { return hypotf(z.re, z.im); }
+static __device__ __forceinline__ bool cfinite(cx<double> z) { return isfinite(z.re) && isfinite(z.im); }
+static __device__ __forceinline__ bool cfinite(cx<float> z) { return isfinite(z.re) && isfinite(z.im); }
+
+// principal logarithm, exp, real power (the reference's std::log / std::pow on
+// complex<double>, srcs/feynman_integral.hpp:310,327,354)
+static __device__ __forceinline__ cx<double> clog_(cx<double> z) { return cmk(log(hypot(z.re, z.im)), atan2(z.im, z.re)); }
+static __device__ __forceinline__ cx<double> cexp_(cx<double> z)
+{
+    double s, c, m = exp(z.re);
+    sincos(z.im, &s, &c);
+    return cmk(m * c, m * s);
+}
+static __device__ __forceinline__ cx<double> cpow_(cx<double> z, double y)
+{
+    double lr = log(hypot(z.re, z.im)), th = atan2(z.im, z.re);
+    double s, c, m = exp(y * lr);
+    sincos(y * th, &s, &c);
+    return cmk(m * c, m * s);
+}
+
+// ------------------------------------------------------------------ conductance-form elimination
+// Reduced Laplacian of the graph with conductances y_e, ground = vertex V-1.
+// Fills the pivots d[k] and the elimination multipliers a[k][i] = c_ki / d_k
+// (i > k), which define L = M^T diag(d) M with M unit upper triangular and
+// M[k][i] = -a[k][i].  Returns the smallest pivot-to-row-size ratio (1 for
+// positive conductances).
+template <class F, class R>
+struct elim {
+    F d[FT_N];
+    F a[FT_N][FT_N];   // a[k][i], i > k
+
+    __device__ __forceinline__ R factor(const F* y)
+    {
+        F c[FT_N][FT_N];   // c[i][j], i < j < N: conductance between i and j
+        F g[FT_N];         // conductance to ground
+#pragma unroll
+        for (int i = 0; i < FT_N; i++) {
+            g[i] = F{};
+#pragma unroll
+            for (int j = 0; j < FT_N; j++) c[i][j] = F{};
+        }
+#pragma unroll
+        for (int e = 0; e < FT_E; e++) {
+            const int k = FT_EK[e], l = FT_EL[e];
+            if (k == FT_V - 1)
+                g[l] = g[l] + y[e];
+            else
+                c[l][k] = c[l][k] + y[e];
+        }
+        R worst = R(1);
+#pragma unroll
+        for (int k = 0; k < FT_N; k++) {
+            F dk = g[k];
+            R mag = mag_of(g[k]);
+#pragma unroll
+            for (int j = k + 1; j < FT_N; j++) {
+                dk = dk + c[k][j];
+                mag += mag_of(c[k][j]);
+            }
+            d[k] = dk;
+            R ratio = mag_of(dk) / mag;
+            worst = ratio < worst ? ratio : worst;
+            F inv = inv_of(dk);
+#pragma unroll
+            for (int i = k + 1; i < FT_N; i++) a[k][i] = c[k][i] * inv;
+#pragma unroll
+            for (int i = k + 1; i < FT_N; i++) {
+                g[i] = g[i] + a[k][i] * g[k];
+#pragma unroll
+                for (int j = i + 1; j < FT_N; j++) c[i][j] = c[i][j] + a[k][i] * c[k][j];
+            }
+        }
+        return worst;
+    }
+
+    // q^T L^{-1} q for a real vector q (forward substitution y = M^-T q, sum y^2/d)
+    template <class Q>
+    __device__ __forceinline__ F quad(const Q* q) const
+    {
+        F y[FT_N];
+        F s = F{};
+#pragma unroll
+        for (int i = 0; i < FT_N; i++) {
+            F yi = from_real((R)q[i]);
+#pragma unroll
+            for (int k = 0; k < i; k++) yi = yi + a[k][i] * y[k];
+            y[i] = yi;
+            s = s + yi * yi * inv_of(d[i]);
+        }
+        return s;
+    }
+
+    static __device__ __forceinline__ R mag_of(R x) { return fabs(x); }
+    static __device__ __forceinline__ R mag_of(cx<R> x) { return fabs(x.re) + fabs(x.im); }
+    static __device__ __forceinline__ R inv_of(R x) { return R(1) / x; }
+    static __device__ __forceinline__ cx<R> inv_of(cx<R> x) { return crecip(x); }
+    static __device__ __forceinline__ F from_real(R x)
+    {
+        F f{};
+        set_real(f, x);
+        return f;
+    }
+    static __device__ __forceinline__ void set_real(R& f, R x) { f = x; }
+    static __device__ __forceinline__ void set_real(cx<R>& f, R x) { f = cmk(x, R(0)); }
+};
+
+// ------------------------------------------------------------------ robust complex LU
+// Complete-pivoting LU of the complex reduced Laplacian (largest modulus, first in
+// column-major order), used when the static elimination reports pivot growth.
+// Returns det and -tr(L^-1 P~).
+static __device__ void robust_complex(const cx<double>* y, const double* prm, cx<double>& det, cx<double>& pphi)
+{
+    cx<double> A[FT_N * FT_N];
+    int rp[FT_N], cp[FT_N];
+    for (int i = 0; i < FT_N * FT_N; i++) A[i] = cmk(0.0, 0.0);
+    for (int e = 0; e < FT_E; e++) {
+        const int k = FT_EK[e], l = FT_EL[e];
+        A[l * FT_N + l] = A[l * FT_N + l] + y[e];
+        if (k == FT_V - 1) continue;
+        A[k * FT_N + k] = A[k * FT_N + k] + y[e];
+        A[k * FT_N + l] = A[k * FT_N + l] - y[e];
+        A[l * FT_N + k] = A[l * FT_N + k] - y[e];
+    }
+    int nt = 0;
+    for (int k = 0; k < FT_N; k++) {
+        int br = k, bc = k;
+        double best = -1.0;
+        for (int c = k; c < FT_N; c++)
+            for (int r = k; r < FT_N; r++) {
+                double s = cabs_(A[r * FT_N + c]);
+                if (s > best) {
+                    best = s;
+                    br = r;
+                    bc = c;
+                }
+            }
+        rp[k] = br;
+        cp[k] = bc;
+        if (br != k) {
+            for (int c = 0; c < FT_N; c++) {
+                cx<double> t = A[k * FT_N + c];
+                A[k * FT_N + c] = A[br * FT_N + c];
+                A[br * FT_N + c] = t;
+            }
+            nt++;
+        }
+        if (bc != k) {
+            for (int r = 0; r < FT_N; r++) {
+                cx<double> t = A[r * FT_N + k];
+                A[r * FT_N + k] = A[r * FT_N + bc];
+                A[r * FT_N + bc] = t;
+            }
+            nt++;
+        }
+        cx<double> inv = crecip(A[k * FT_N + k]);
+        for (int r = k + 1; r < FT_N; r++) A[r * FT_N + k] = A[r * FT_N + k] * inv;
+        for (int r = k + 1; r < FT_N; r++)
+            for (int c = k + 1; c < FT_N; c++) A[r * FT_N + c] = A[r * FT_N + c] - A[r * FT_N + k] * A[k * FT_N + c];
+    }
+    det = cmk(1.0, 0.0);
+    for (int i = 0; i < FT_N; i++) det = det * A[i * FT_N + i];
+    if (nt & 1) det = cmk(-det.re, -det.im);
+    // -tr(L^-1 P~), P~ = sum_r sigma_r q_r q_r^T: sum_r sigma_r q_r^T L^-1 q_r
+    cx<double> tr = cmk(0.0, 0.0);
+    for (int r = 0; r < FT_RANK; r++) {
+        cx<double> b[FT_N];
+        for (int i = 0; i < FT_N; i++) b[i] = cmk(prm[P_Q + r * FT_N + i], 0.0);
+        for (int k = 0; k < FT_N; k++) {
+            cx<double> t = b[k];
+            b[k] = b[rp[k]];
+            b[rp[k]] = t;
+        }
+        for (int i = 0; i < FT_N; i++)
+            for (int j = 0; j < i; j++) b[i] = b[i] - A[i * FT_N + j] * b[j];
+        for (int i = FT_N - 1; i >= 0; i--) {
+            for (int j = i + 1; j < FT_N; j++) b[i] = b[i] - A[i * FT_N + j] * b[j];
+            b[i] = b[i] * crecip(A[i * FT_N + i]);
+        }
+        for (int k = FT_N - 1; k >= 0; k--) {
+            cx<double> t = b[k];
+            b[k] = b[cp[k]];
+            b[cp[k]] = t;
+        }
+        cx<double> s = cmk(0.0, 0.0);
+        for (int i = 0; i < FT_N; i++) s = s + prm[P_Q + r * FT_N + i] * b[i];
+        tr = tr + prm[P_SIG + r] * s;
+    }
+    pphi = cmk(-tr.re, -tr.im);
+}
+
+// ------------------------------------------------------------------ sector draw, FP64
+struct table_ref {
+    const void* w;              // staged copies (shared memory): w, Jr, 1/r in the working precision
+    const void* Jr;
+    const void* ri;
+    const unsigned char* meta;  // mm << 7 | loop number
+    const unsigned char* gm;    // global copy (FP64 sections for exact re-checks)
+};
+
+static __device__ __forceinline__ void draw_sector64(xo& g, const table_ref& t, double Jr_full, double* X, double& F,
+                                                     double& Gv, unsigned char* ord)
+{
+    const double* w = (const double*)t.w;
+    const double* Jr = (const double*)t.Jr;
+    const double* ri = (const double*)t.ri;
+    const unsigned char* meta = t.meta;
+    u32 sub = FT_FULL;
+    double JJr = Jr_full, XX = 1.0;
+    bool MM = true;
+    int oL = FT_LOOPS;
+    F = 1.0;
+    Gv = 0.0;
+#pragma unroll
+    for (int j = 0; j < FT_E; j++) {
+        const double R = u01(g.next()) * JJr;
+        double T = 0.0;
+        int e = 0;
+        bool found = false;
+#pragma unroll
+        for (int c = 0; c < FT_E; c++) {
+            if (((sub >> c) & 1u) && !found) {
+                T += w[sub ^ (1u << c)];
+                e = c;
+                found = T > R;
+            }
+        }
+        sub ^= 1u << e;
+        JJr = Jr[sub];
+        const double rinv = ri[sub];
+        const unsigned m = meta[sub];
+        const bool mm = (m >> 7) != 0;
+        const int L = (int)(m & 127u);
+        if (MM && !mm) Gv = XX;
+        MM = mm;
+#pragma unroll
+        for (int k = 0; k < FT_E; k++)
+            if (k == e) X[k] = XX;
+        if (L < oL) {
+            F *= XX;
+            oL = L;
+        }
+        if (FT_RECORD) ord[j] = (unsigned char)e;
+        if (j < FT_E - 1) XX *= pow(1.0 - u01(g.next()), rinv);
+    }
+}
+
+// ------------------------------------------------------------------ sector draw, mixed
+// two-float value hi + lo
+struct f2 {
+    float hi, lo;
+};
+static __device__ __forceinline__ f2 f2_add(f2 a, float b)
+{
+    float s = a.hi + b;
+    float bb = s - a.hi;
+    float err = (a.hi - (s - bb)) + (b - bb);
+    float lo = a.lo + err;
+    float h = s + lo;
+    f2 r;
+    r.hi = h;
+    r.lo = lo - (h - s);
+    return r;
+}
+static __device__ __forceinline__ f2 f2_add2(f2 a, f2 b)
+{
+    f2 r = f2_add(a, b.hi);
+    return f2_add(r, b.lo);
+}
+
+// log(1 - u) for u = (x >> 11) 2^-53, to a few 1e-8 absolute
+static __device__ __forceinline__ f2 log1m_u(u64 x)
+{
+    const u64 m = x >> 11;
+    f2 r;
+    if (m < (1ull << 52)) {
+        // u < 1/2: log1p(-u), u rounded to float (relative 2^-24 -> absolute < 2^-24)
+        r.hi = log1pf(-__ull2float_rn(m) * 0x1.0p-53f);
+        r.lo = 0.0f;
+        return r;
+    }
+    // 1 - u = q 2^-53 with q < 2^52 exact; q rounded to float = 2^k (1 + f),
+    // log(1 - u) = (k - 53) ln2 + log1p(f) with f exact
+    const u64 q = (1ull << 53) - m;
+    const float qf = __ull2float_rn(q);
+    const int bits = __float_as_int(qf);
+    const int k = ((bits >> 23) & 0xff) - 127;
+    const float f = __int_as_float((bits & 0x007fffff) | 0x3f800000) - 1.0f;
+    const float kk = (float)(k - 53);
+    // ln2 split so that kk * LN2_HI is exact
+    const float LN2_HI = 0.693145751953125f, LN2_LO = 1.42860682030941723212e-6f;
+    f2 a;
+    a.hi = kk * LN2_HI;
+    a.lo = kk * LN2_LO;
+    return f2_add(a, log1pf(f));
+}
+
+static __device__ __forceinline__ int draw_sector32(xo& g, const table_ref& t, const float* pf, f2* lx, f2& lF,
+                                                    f2& lG, unsigned char* ord)
+{
+    const float* w = (const float*)t.w;
+    const float* Jr = (const float*)t.Jr;
+    const float* ri = (const float*)t.ri;
+    const unsigned char* meta = t.meta;
+    u32 sub = FT_FULL;
+    float JJr = pf[P_JRFULL];
+    bool MM = true;
+    int oL = FT_LOOPS, exact = 0;
+    f2 lxx;
+    lxx.hi = lxx.lo = 0.0f;
+    lF = lxx;
+    lG = lxx;
+#pragma unroll
+    for (int j = 0; j < FT_E; j++) {
+        const u64 x = g.next();
+        // FP32 decision with margin: |T32 - T64| <= (2E) 2^-24 Jr, |R32 - R64| <= 4 2^-24 Jr
+        const float uf = (float)(u32)(x >> 40) * 0x1.0p-24f;
+        const float Rf = uf * JJr;
+        const float margin = (float)(2 * FT_E + 8) * 0x1.0p-24f * JJr;
+        float T = 0.0f;
+        int e = 0, sure = -1;
+        bool unsure = false;
+#pragma unroll
+        for (int c = 0; c < FT_E; c++) {
+            if (((sub >> c) & 1u) && sure < 0) {
+                T += w[sub ^ (1u << c)];
+                e = c;
+                const float d = T - Rf;
+                if (d > margin)
+                    sure = c;
+                else if (d >= -margin)
+                    unsure = true;
+            }
+        }
+        int cut = sure >= 0 ? sure : e;
+        if (unsure) {
+            // repeat the comparison exactly as the reference does it, in FP64
+            const double* w64 = (const double*)(t.gm + T_W64);
+            const double* Jr64 = (const double*)(t.gm + T_JR64);
+            const double R = u01(x) * Jr64[sub];
+            double TT = 0.0;
+            bool found = false;
+            for (int c = 0; c < FT_E; c++) {
+                if (((sub >> c) & 1u) && !found) {
+                    TT += w64[sub ^ (1u << c)];
+                    cut = c;
+                    found = TT > R;
+                }
+            }
+            exact++;
+        }
+        sub ^= 1u << cut;
+        JJr = Jr[sub];
+        const float rinv = ri[sub];
+        const unsigned m = meta[sub];
+        const bool mm = (m >> 7) != 0;
+        const int L = (int)(m & 127u);
+        if (MM && !mm) lG = lxx;
+        MM = mm;
+#pragma unroll
+        for (int k = 0; k < FT_E; k++)
+            if (k == cut) lx[k] = lxx;
+        if (L < oL) {
+            lF = f2_add2(lF, lxx);
+            oL = L;
+        }
+        if (FT_RECORD) ord[j] = (unsigned char)cut;
+        if (j < FT_E - 1) {
+            f2 l = log1m_u(g.next());
+            // (hi + lo) * rinv with the product error kept
+            float p = l.hi * rinv;
+            float pe = fmaf(l.hi, rinv, -p) + l.lo * rinv;
+            f2 inc;
+            inc.hi = p;
+            inc.lo = pe;
+            lxx = f2_add2(lxx, inc);
+        }
+    }
+    return exact;
+}
+
+// ------------------------------------------------------------------ integrand, FP64
+// X: unnormalised sector point; returns R per eps order, false when dropped.
+// `robust` reports that the complete-pivoting LU was needed.
+static __device__ __forceinline__ bool integrand64(const double* prm, double* X, double psi_tr, double xi_tr,
+                                                   cx<double>* out, bool& robust)
+{
+    const double D = prm[P_D], W = prm[P_W], IGtr = prm[P_IGTR];
+    // normalise so that psi_tr^(-D/2) (psi_tr/xi_tr)^W = 1 (srcs/feynman_integral.hpp:201-204)
+    const double tgt = pow(psi_tr, -D / 2.) * pow(psi_tr / xi_tr, W);
+    const double scale = pow(tgt, prm[P_NORM]);
+    double Xi[FT_E];
+    double Xprod = 1.0;
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        X[e] *= scale;
+        Xi[e] = 1.0 / X[e];
+        Xprod *= X[e];
+    }
+    elim<double, double> L;
+    L.factor(Xi);
+    double det = 1.0;
+#pragma unroll
+    for (int k = 0; k < FT_N; k++) det *= L.d[k];
+    robust = false;
+#if FT_MODE == 0
+    const double psi = det * Xprod;
+    double R = IGtr * pow(psi, -D / 2.);
+    if (!isfinite(R)) return false;
+#if FT_ONLY_PSI
+    out[0] = cmk(R, 0.0);
+    return true;
+#else
+    double tr = 0.0;
+#pragma unroll
+    for (int r = 0; r < FT_RANK; r++) tr += prm[P_SIG + r] * L.quad(prm + P_Q + r * FT_N);
+    double pxi = -tr;
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) pxi += prm[P_M2 + e] * X[e];
+    R *= pow(pxi, -W);
+    if (!isfinite(R)) return false;
+    out[0] = cmk(R, 0.0);
+    if (FT_K > 1) {
+        const double ef = log(psi) - FT_LOOPS * log(pxi);
+#pragma unroll
+        for (int j = 1; j < FT_K; j++) {
+            R *= ef / (double)j;
+            out[j] = cmk(R, 0.0);
+        }
+    }
+    return true;
+#endif
+#else
+    const double kappa = prm[P_DEF];
+    // G = L^-1 = N diag(1/d) N^T with N = M^-1 (entrywise non-negative)
+    double Nm[FT_N][FT_N];
+#pragma unroll
+    for (int i = FT_N - 1; i >= 0; i--) {
+#pragma unroll
+        for (int j = 0; j < FT_N; j++) Nm[i][j] = 0.0;
+        Nm[i][i] = 1.0;
+#pragma unroll
+        for (int j = i + 1; j < FT_N; j++) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = i + 1; k <= j; k++) s += L.a[i][k] * Nm[k][j];
+            Nm[i][j] = s;
+        }
+    }
+    double id[FT_N];
+#pragma unroll
+    for (int k = 0; k < FT_N; k++) id[k] = 1.0 / L.d[k];
+    double G[FT_N][FT_N];
+#pragma unroll
+    for (int i = 0; i < FT_N; i++)
+#pragma unroll
+        for (int j = i; j < FT_N; j++) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = j; k < FT_N; k++) s += Nm[i][k] * Nm[j][k] * id[k];
+            G[i][j] = s;
+            G[j][i] = s;
+        }
+    // h_r = L^-1 q_r; per edge: hb[r][e] = h_r . b_e with b_e = e_k - e_l (ground row zero)
+    double hb[FT_RANK][FT_E];
+#pragma unroll
+    for (int r = 0; r < FT_RANK; r++) {
+        double h[FT_N];
+#pragma unroll
+        for (int i = 0; i < FT_N; i++) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < FT_N; j++) s += G[i][j] * prm[P_Q + r * FT_N + j];
+            h[i] = s;
+        }
+#pragma unroll
+        for (int e = 0; e < FT_E; e++) {
+            const int k = FT_EK[e], l = FT_EL[e];
+            hb[r][e] = (k == FT_V - 1 ? 0.0 : h[k]) - h[l];
+        }
+    }
+    // s_ab = sum_r sigma_r hb_a hb_b, t_ab = b_a^T G b_b
+    auto Gx = [&](int i, int j) -> double { return (i == FT_V - 1 || j == FT_V - 1) ? 0.0 : G[i][j]; };
+    double dphi[FT_E];
+    double H[FT_E][FT_E];
+#pragma unroll
+    for (int a = 0; a < FT_E; a++) {
+        const int ka = FT_EK[a], la = FT_EL[a];
+        double s = 0.0;
+#pragma unroll
+        for (int r = 0; r < FT_RANK; r++) s += prm[P_SIG + r] * hb[r][a] * hb[r][a];
+        const double t = Gx(ka, ka) + Gx(la, la) - 2.0 * Gx(ka, la);
+        const double xa = Xi[a] * Xi[a];
+        const double xas = xa * s;
+        dphi[a] = -xas;
+        H[a][a] = 2.0 * xas * (Xi[a] - xa * t);
+#pragma unroll
+        for (int b = a + 1; b < FT_E; b++) {
+            const int kb = FT_EK[b], lb = FT_EL[b];
+            double s2 = 0.0;
+#pragma unroll
+            for (int r = 0; r < FT_RANK; r++) s2 += prm[P_SIG + r] * hb[r][a] * hb[r][b];
+            const double t2 = Gx(ka, kb) + Gx(la, lb) - Gx(ka, lb) - Gx(la, kb);
+            H[a][b] = -2.0 * xa * (Xi[b] * Xi[b]) * s2 * t2;
+        }
+    }
+    // deformation x -> x exp(i theta), theta = -lambda (d(phi/psi)/dx + m^2)
+    double theta[FT_E];
+    cx<double> cX[FT_E], cy[FT_E];
+    double xnu = 0.0;
+    cx<double> cXprod = cmk(1.0, 0.0);
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        theta[e] = (dphi[e] + prm[P_M2 + e]) * kappa;
+        double sn, cs;
+        sincos(theta[e], &sn, &cs);
+        cX[e] = cmk(X[e] * cs, X[e] * sn);
+        cy[e] = cmk(Xi[e] * cs, -Xi[e] * sn);   // 1 / cX
+        xnu += prm[P_NU + e] * theta[e];
+        cXprod = cXprod * cX[e];
+    }
+    elim<cx<double>, double> CL;
+    const double growth = CL.factor(cy);
+    cx<double> cdet, cpphi;
+    if (growth > 1e-8) {
+        cdet = cmk(1.0, 0.0);
+#pragma unroll
+        for (int k = 0; k < FT_N; k++) cdet = cdet * CL.d[k];
+        cx<double> tr = cmk(0.0, 0.0);
+#pragma unroll
+        for (int r = 0; r < FT_RANK; r++) tr = tr + prm[P_SIG + r] * CL.quad(prm + P_Q + r * FT_N);
+        cpphi = cmk(-tr.re, -tr.im);
+    } else {
+        robust = true;
+        robust_complex(cy, prm, cdet, cpphi);
+    }
+    const cx<double> cPsi = cXprod * cdet;
+    cx<double> cR = IGtr * cpow_(cPsi, -D / 2.);
+    // det(I + i kappa X^1/2 H X^1/2), symmetric elimination without pivoting
+    cx<double> J[FT_E][FT_E];
+    double sx[FT_E];
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) sx[e] = sqrt(X[e]);
+#pragma unroll
+    for (int a = 0; a < FT_E; a++)
+#pragma unroll
+        for (int b = a; b < FT_E; b++) J[a][b] = cmk(a == b ? 1.0 : 0.0, kappa * H[a][b] * sx[a] * sx[b]);
+    cx<double> detJ = cmk(1.0, 0.0);
+#pragma unroll
+    for (int k = 0; k < FT_E; k++) {
+        const cx<double> piv = J[k][k];
+        detJ = detJ * piv;
+        const cx<double> inv = crecip(piv);
+#pragma unroll
+        for (int i = k + 1; i < FT_E; i++) {
+            const cx<double> f = J[k][i] * inv;
+#pragma unroll
+            for (int j = i; j < FT_E; j++) J[i][j] = J[i][j] - f * J[k][j];
+        }
+    }
+    double sn, cs;
+    sincos(xnu, &sn, &cs);
+    cR = cR * (detJ * cmk(cs, sn));
+    cx<double> cPXi = cpphi;
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) cPXi = cPXi + prm[P_M2 + e] * cX[e];
+    cR = cR * cpow_(cPXi, -W);
+    if (!cfinite(cR)) return false;
+    out[0] = cR;
+    if (FT_K > 1) {
+        const cx<double> lp = clog_(cPsi), lv = clog_(cPXi);
+        const cx<double> ef = cmk(lp.re - FT_LOOPS * lv.re, lp.im - FT_LOOPS * lv.im);
+#pragma unroll
+        for (int j = 1; j < FT_K; j++) {
+            cR = cR * ((1.0 / (double)j) * ef);
+            out[j] = cR;
+        }
+    }
+    return true;
+#endif
+}
+
+
+// ------------------------------------------------------------------ integrand, mixed
+#if FT_PREC == 1
+// positive value m * 2^e with m in [1, 2): products of many pivots and X values
+// without overflow, and logarithms split into an exact integer and a small part
+struct mexp {
+    float m;
+    int e;
+    bool bad;
+};
+static __device__ __forceinline__ void mx_mul(mexp& a, float x)
+{
+    const float p = a.m * x;
+    const int b = __float_as_int(p);
+    const int be = (b >> 23) & 0xff;
+    a.bad |= (be == 0) | (be == 255) | (b < 0);
+    a.e += be - 127;
+    a.m = __int_as_float((b & 0x007fffff) | 0x3f800000);
+}
+static __device__ __forceinline__ mexp mx_one()
+{
+    mexp r;
+    r.m = 1.0f;
+    r.e = 0;
+    r.bad = false;
+    return r;
+}
+static __device__ __forceinline__ f2 f2_make(float h, float l)
+{
+    f2 r;
+    r.hi = h;
+    r.lo = l;
+    return r;
+}
+static __device__ __forceinline__ f2 f2_mulf(f2 a, float b)
+{
+    const float p = a.hi * b;
+    const float e = fmaf(a.hi, b, -p) + a.lo * b;
+    const float h = p + e;
+    return f2_make(h, e - (h - p));
+}
+static __device__ __forceinline__ f2 f2_mul2(f2 a, f2 b)
+{
+    const float p = a.hi * b.hi;
+    const float e = fmaf(a.hi, b.hi, -p) + (a.hi * b.lo + a.lo * b.hi);
+    const float h = p + e;
+    return f2_make(h, e - (h - p));
+}
+static __device__ __forceinline__ f2 f2_neg(f2 a) { return f2_make(-a.hi, -a.lo); }
+#define RLN2_HI 1.44269502162933349609375f
+#define RLN2_LO 1.925963033500011e-8f
+#define LN2_F 0.69314718055994531f
+
+// log2(value / exp(lref)) for value = mx and a natural-log reference lref (two-float)
+static __device__ __forceinline__ f2 log2_ratio(const mexp& mx, f2 lref)
+{
+    f2 r = f2_mul2(lref, f2_make(RLN2_HI, RLN2_LO));
+    r = f2_add(f2_neg(r), (float)mx.e);
+    return f2_add(r, log2f(mx.m));
+}
+
+// principal argument reduced to (-pi, pi]; `edge` reports a value within 1e-5 of
+// the branch cut, where FP32 cannot decide the branch the way the reference does
+static __device__ __forceinline__ float wrap_pi(float x, bool& edge)
+{
+    const float TWO_PI_HI = 6.28318548202514648f, TWO_PI_LO = -1.7484555e-7f;
+    const float k = rintf(x * 0.159154943091895336f);
+    float r = fmaf(-k, TWO_PI_HI, x);
+    r = fmaf(-k, TWO_PI_LO, r);
+    edge |= fabsf(r) > 3.14158265f;
+    return r;
+}
+
+static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx, f2 lF, f2 lG, cx<float>* out,
+                                                   bool& need64)
+{
+    need64 = false;
+    const float D2 = 0.5f * pf[P_D], W = pf[P_W];
+    // working frame X_e = exp(lx_e - sh), sh an integer near the middle of the range;
+    // R and the eps factor are ratios to the tropical approximants and do not depend on it
+    float lmin = 0.0f;
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) lmin = fminf(lmin, lx[e].hi);
+    const float sh = rintf(0.5f * lmin);
+    float X[FT_E], Xi[FT_E];
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        const f2 a = f2_add(lx[e], -sh);
+        const float ep = expf(a.hi), em = expf(-a.hi);
+        X[e] = fmaf(ep, a.lo, ep);
+        Xi[e] = fmaf(em, -a.lo, em);
+    }
+    const f2 lFs = f2_add(lF, -(float)FT_LOOPS * sh);   // log psi_tr in the frame
+    const f2 lGs = f2_add(lG, -sh);                      // log V_tr = log(xi_tr / psi_tr)
+    elim<float, float> L;
+    L.factor(Xi);
+    mexp psi = mx_one();
+#pragma unroll
+    for (int k = 0; k < FT_N; k++) mx_mul(psi, L.d[k]);
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) mx_mul(psi, X[e]);
+    if (psi.bad) {
+        need64 = true;
+        return false;
+    }
+    const float IGtr = pf[P_IGTR];
+#if FT_MODE == 0
+    const f2 lpsi = log2_ratio(psi, lFs);   // log2(psi / psi_tr)
+#if FT_ONLY_PSI
+    const f2 t = f2_mulf(lpsi, -D2);
+    const float R = exp2f(t.hi) * (1.0f + t.lo * LN2_F);
+    out[0] = cmk(IGtr * R, 0.0f);
+    return true;
+#else
+    float pphi = 0.0f, mag = 0.0f;
+#pragma unroll
+    for (int r = 0; r < FT_RANK; r++) {
+        const float v = pf[P_SIG + r] * L.quad(pf + P_Q + r * FT_N);
+        pphi -= v;
+        mag += fabsf(v);
+    }
+    float pxi = pphi;
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        const float v = pf[P_M2 + e] * X[e];
+        pxi += v;
+        mag += fabsf(v);
+    }
+    if (!(pxi > 1e-3f * mag)) {   // cancellation, or a sign the FP64 pass must judge
+        need64 = true;
+        return false;
+    }
+    mexp V = mx_one();
+    mx_mul(V, pxi);
+    const f2 lv = log2_ratio(V, lGs);   // log2(V / V_tr)
+    const f2 t = f2_add2(f2_mulf(lpsi, -D2), f2_mulf(lv, -W));
+    const float Rf = exp2f(t.hi) * (1.0f + t.lo * LN2_F);
+    if (!isfinite(Rf) || V.bad) {
+        need64 = true;
+        return false;
+    }
+    float R = IGtr * Rf;
+    out[0] = cmk(R, 0.0f);
+    if (FT_K > 1) {
+        const float ef = LN2_F * ((float)(psi.e - FT_LOOPS * V.e) + (log2f(psi.m) - (float)FT_LOOPS * log2f(V.m)));
+#pragma unroll
+        for (int j = 1; j < FT_K; j++) {
+            R *= ef / (float)j;
+            out[j] = cmk(R, 0.0f);
+        }
+    }
+    return true;
+#endif
+#else
+    const float kappa = pf[P_DEF];
+    // G = L^-1 = N diag(1/d) N^T, N = M^-1 (entrywise non-negative)
+    float Nm[FT_N][FT_N];
+#pragma unroll
+    for (int i = FT_N - 1; i >= 0; i--) {
+#pragma unroll
+        for (int j = 0; j < FT_N; j++) Nm[i][j] = 0.0f;
+        Nm[i][i] = 1.0f;
+#pragma unroll
+        for (int j = i + 1; j < FT_N; j++) {
+            float s = 0.0f;
+#pragma unroll
+            for (int k = i + 1; k <= j; k++) s = fmaf(L.a[i][k], Nm[k][j], s);
+            Nm[i][j] = s;
+        }
+    }
+    float id[FT_N];
+#pragma unroll
+    for (int k = 0; k < FT_N; k++) id[k] = 1.0f / L.d[k];
+    float G[FT_N][FT_N];
+#pragma unroll
+    for (int i = 0; i < FT_N; i++)
+#pragma unroll
+        for (int j = i; j < FT_N; j++) {
+            float s = 0.0f;
+#pragma unroll
+            for (int k = j; k < FT_N; k++) s = fmaf(Nm[i][k] * Nm[j][k], id[k], s);
+            G[i][j] = s;
+            G[j][i] = s;
+        }
+    float hb[FT_RANK][FT_E];
+#pragma unroll
+    for (int r = 0; r < FT_RANK; r++) {
+        float h[FT_N];
+#pragma unroll
+        for (int i = 0; i < FT_N; i++) {
+            float s = 0.0f;
+#pragma unroll
+            for (int j = 0; j < FT_N; j++) s = fmaf(G[i][j], pf[P_Q + r * FT_N + j], s);
+            h[i] = s;
+        }
+#pragma unroll
+        for (int e = 0; e < FT_E; e++) {
+            const int k = FT_EK[e], l = FT_EL[e];
+            hb[r][e] = (k == FT_V - 1 ? 0.0f : h[k]) - h[l];
+        }
+    }
+    auto Gx = [&](int i, int j) -> float { return (i == FT_V - 1 || j == FT_V - 1) ? 0.0f : G[i][j]; };
+    float theta[FT_E];
+    float H[FT_E][FT_E];
+#pragma unroll
+    for (int a = 0; a < FT_E; a++) {
+        const int ka = FT_EK[a], la = FT_EL[a];
+        float s = 0.0f;
+#pragma unroll
+        for (int r = 0; r < FT_RANK; r++) s = fmaf(pf[P_SIG + r] * hb[r][a], hb[r][a], s);
+        const float t = Gx(ka, ka) + Gx(la, la) - 2.0f * Gx(ka, la);
+        const float xa = Xi[a] * Xi[a];
+        const float xas = xa * s;
+        theta[a] = (-xas + pf[P_M2 + a]) * kappa;
+        H[a][a] = 2.0f * xas * (Xi[a] - xa * t);
+#pragma unroll
+        for (int b = a + 1; b < FT_E; b++) {
+            const int kb = FT_EK[b], lb = FT_EL[b];
+            float s2 = 0.0f;
+#pragma unroll
+            for (int r = 0; r < FT_RANK; r++) s2 = fmaf(pf[P_SIG + r] * hb[r][a], hb[r][b], s2);
+            const float t2 = Gx(ka, kb) + Gx(la, lb) - Gx(ka, lb) - Gx(la, kb);
+            H[a][b] = -2.0f * xa * (Xi[b] * Xi[b]) * s2 * t2;
+        }
+    }
+    cx<float> cX[FT_E], cy[FT_E];
+    float xnu = 0.0f, thsum = 0.0f;
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        float sn, cs;
+        sincosf(theta[e], &sn, &cs);
+        cX[e] = cmk(X[e] * cs, X[e] * sn);
+        cy[e] = cmk(Xi[e] * cs, -Xi[e] * sn);
+        xnu = fmaf(pf[P_NU + e], theta[e], xnu);
+        thsum += theta[e];
+    }
+    elim<cx<float>, float> CL;
+    const float growth = CL.factor(cy);
+    if (!(growth > 1e-3f)) {
+        need64 = true;
+        return false;
+    }
+    // |cPsi| = prod X * prod |d_k|, arg cPsi = sum theta + sum arg d_k
+    mexp cpsi = mx_one();
+    cx<float> ph = cmk(1.0f, 0.0f);
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) mx_mul(cpsi, X[e]);
+#pragma unroll
+    for (int k = 0; k < FT_N; k++) {
+        const float m = cabs_(CL.d[k]);
+        mx_mul(cpsi, m);
+        const float im = 1.0f / m;
+        ph = ph * cmk(CL.d[k].re * im, CL.d[k].im * im);
+    }
+    bool edge = false;
+    const float apsi = wrap_pi(thsum + atan2f(ph.im, ph.re), edge);
+    // phi/psi of the deformed point and the deformed V
+    cx<float> cpphi = cmk(0.0f, 0.0f);
+    float mag = 0.0f;
+#pragma unroll
+    for (int r = 0; r < FT_RANK; r++) {
+        const cx<float> v = pf[P_SIG + r] * CL.quad(pf + P_Q + r * FT_N);
+        cpphi = cpphi - v;
+        mag += cabs_(v);
+    }
+    cx<float> cV = cpphi;
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        cV = cV + pf[P_M2 + e] * cX[e];
+        mag += pf[P_M2 + e] * X[e];
+    }
+    const float vabs = cabs_(cV);
+    if (!(vabs > 1e-3f * mag)) {
+        need64 = true;
+        return false;
+    }
+    mexp mv = mx_one();
+    mx_mul(mv, vabs);
+    const float av = atan2f(cV.im, cV.re);
+    edge |= fabsf(av) > 3.14158265f;
+    // det(I + i kappa X^1/2 H X^1/2)
+    cx<float> J[FT_E][FT_E];
+    float sx[FT_E];
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) sx[e] = sqrtf(X[e]);
+#pragma unroll
+    for (int a = 0; a < FT_E; a++)
+#pragma unroll
+        for (int b = a; b < FT_E; b++) J[a][b] = cmk(a == b ? 1.0f : 0.0f, kappa * H[a][b] * sx[a] * sx[b]);
+    mexp mj = mx_one();
+    cx<float> pj = cmk(1.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < FT_E; k++) {
+        const cx<float> piv = J[k][k];
+        const float m = cabs_(piv);
+        mx_mul(mj, m);
+        const float im = 1.0f / m;
+        pj = pj * cmk(piv.re * im, piv.im * im);
+        const cx<float> inv = crecip(piv);
+#pragma unroll
+        for (int i = k + 1; i < FT_E; i++) {
+            const cx<float> f = J[k][i] * inv;
+#pragma unroll
+            for (int j = i; j < FT_E; j++) J[i][j] = J[i][j] - f * J[k][j];
+        }
+    }
+    if (edge || cpsi.bad || mv.bad || mj.bad) {
+        need64 = true;
+        return false;
+    }
+    // log2|cR / IGtr| and arg cR
+    const f2 lpsi = log2_ratio(cpsi, lFs);
+    const f2 lv = log2_ratio(mv, lGs);
+    f2 t = f2_add2(f2_mulf(lpsi, -D2), f2_mulf(lv, -W));
+    t = f2_add(t, (float)mj.e);
+    t = f2_add(t, log2f(mj.m));
+    const float ang = -D2 * apsi + atan2f(pj.im, pj.re) + xnu - W * av;
+    const float mod = exp2f(t.hi) * (1.0f + t.lo * LN2_F);
+    float sn, cs;
+    sincosf(ang, &sn, &cs);
+    if (!isfinite(mod)) {
+        need64 = true;
+        return false;
+    }
+    cx<float> c = cmk(IGtr * mod * cs, IGtr * mod * sn);
+    out[0] = c;
+    if (FT_K > 1) {
+        const float er =
+            LN2_F * ((float)(cpsi.e - FT_LOOPS * mv.e) + (log2f(cpsi.m) - (float)FT_LOOPS * log2f(mv.m)));
+        const float ei = apsi - (float)FT_LOOPS * av;
+#pragma unroll
+        for (int j = 1; j < FT_K; j++) {
+            c = c * cmk(er / (float)j, ei / (float)j);
+            out[j] = c;
+        }
+    }
+    return true;
+#endif
+}
+#endif
+
+// ------------------------------------------------------------------ accumulation
+// Neumaier-compensated running sums per thread
+struct nsum {
+    double s, c;
+    __device__ __forceinline__ void add(double v)
+    {
+        double t = s + v;
+        c += (fabs(s) >= fabs(v)) ? ((s - t) + v) : ((v - t) + s);
+        s = t;
+    }
+};
+
+// double-double sum of two (hi, lo) pairs
+static __device__ __forceinline__ void dd_add(double& ah, double& al, double bh, double bl)
+{
+    double s = ah + bh;
+    double bb = s - ah;
+    double err = (ah - (s - bb)) + (bh - bb);
+    err += al + bl;
+    ah = s + err;
+    al = err - (ah - s);
+}
+
+// Block reduction of per-thread (hi, lo) accumulators into acc_out[blockIdx.x]
+static __device__ void block_reduce(double* vals /* ACC_SLOTS per thread, (hi,lo) pairs for the first 8K */,
+                                    double* acc_out)
+{
+    __shared__ double red[FT_BLOCK / 32][ACC_SLOTS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int s = 0; s < 8 * FT_K; s += 2) {
+        double h = vals[s], l = vals[s + 1];
+#pragma unroll
+        for (int off = 16; off; off >>= 1) {
+            double oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
+            dd_add(h, l, oh, ol);
+        }
+        if (lane == 0) {
+            red[wid][s] = h;
+            red[wid][s + 1] = l;
+        }
+    }
+    for (int s = 8 * FT_K; s < ACC_SLOTS; s++) {
+        double v = vals[s];
+#pragma unroll
+        for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[wid][s] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double* o = acc_out + (size_t)blockIdx.x * ACC_SLOTS;
+        for (int s = 0; s < 8 * FT_K; s += 2) {
+            double h = red[0][s], l = red[0][s + 1];
+            for (int w = 1; w < FT_BLOCK / 32; w++) dd_add(h, l, red[w][s], red[w][s + 1]);
+            o[s] = h;
+            o[s + 1] = l;
+        }
+        for (int s = 8 * FT_K; s < ACC_SLOTS; s++) {
+            double v = 0.0;
+            for (int w = 0; w < FT_BLOCK / 32; w++) v += red[w][s];
+            o[s] = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ lane start states
+// state <- P_b state for every set bit b of `lane`, with P_b = (T^S)^(2^b) supplied by
+// the host (S = draws per lane).  The loop is uniform across the warp so that the
+// matrix columns are broadcast loads.
+static __device__ __forceinline__ void skip_lanes(xo& g, u32 lane, const u64* __restrict__ pw, int nbits)
+{
+    for (int b = 0; b < nbits; b++) {
+        const bool mine = (lane >> b) & 1u;
+        if (!__any_sync(0xffffffffu, mine)) continue;
+        const ulonglong2* M = (const ulonglong2*)(pw + (size_t)b * 1024);
+        u64 r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+        const u64 sv[4] = {g.a, g.b, g.c, g.d};
+#pragma unroll 4
+        for (int c = 0; c < 256; c++) {
+            const u64 mask = 0ull - ((sv[c >> 6] >> (c & 63)) & 1ull);
+            const ulonglong2 lo = __ldg(M + 2 * c), hi = __ldg(M + 2 * c + 1);
+            r0 ^= lo.x & mask;
+            r1 ^= lo.y & mask;
+            r2 ^= hi.x & mask;
+            r3 ^= hi.y & mask;
+        }
+        if (mine) {
+            g.a = r0;
+            g.b = r1;
+            g.c = r2;
+            g.d = r3;
+        }
+    }
+}
+
+// ------------------------------------------------------------------ table staging
+// FP64 form: shared = [w64 | Jr64 | 1/r64 | meta] (25 bytes per entry, the global
+// layout's first sections).  Mixed form: shared = [w32 | Jr32 | 1/r32 | meta].
+#if FT_PREC == 0
+#define SM_BYTES (25u * T_ENTRIES)
+#else
+#define SM_BYTES (13u * T_ENTRIES)
+#endif
+static __device__ __forceinline__ void copy_bytes(unsigned char* dst, const unsigned char* __restrict__ src, u32 bytes)
+{
+    const u32 n16 = bytes / 16u;
+    for (u32 i = threadIdx.x; i < n16; i += blockDim.x) ((uint4*)dst)[i] = ((const uint4*)src)[i];
+    for (u32 i = n16 * 16u + threadIdx.x; i < bytes; i += blockDim.x) dst[i] = src[i];
+}
+
+static __device__ __forceinline__ table_ref stage_table(unsigned char* sm, const unsigned char* __restrict__ tab)
+{
+    table_ref t;
+    t.gm = tab;
+#if FT_TABLE_GLOBAL
+    // large tables stay in global memory (L2 / L1 cached)
+    (void)sm;
+#if FT_PREC == 0
+    t.w = tab + T_W64;
+    t.Jr = tab + T_JR64;
+    t.ri = tab + T_RI64;
+#else
+    t.w = tab + T_W32;
+    t.Jr = tab + T_JR32;
+    t.ri = tab + T_RI32;
+#endif
+    t.meta = tab + T_META;
+    return t;
+#endif
+#if FT_PREC == 0
+    copy_bytes(sm, tab, 25u * T_ENTRIES);
+    t.w = sm + T_W64;
+    t.Jr = sm + T_JR64;
+    t.ri = sm + T_RI64;
+    t.meta = sm + T_META;
+#else
+    copy_bytes(sm, tab + T_F32, 12u * T_ENTRIES);
+    copy_bytes(sm + 12u * T_ENTRIES, tab + T_META, T_ENTRIES);
+    t.w = sm;
+    t.Jr = sm + 4u * T_ENTRIES;
+    t.ri = sm + 8u * T_ENTRIES;
+    t.meta = sm + 12u * T_ENTRIES;
+#endif
+    __syncthreads();
+    return t;
+}
+
+// ------------------------------------------------------------------ per-thread accumulators
+struct accum {
+    nsum S[4 * FT_K];   // re S1, re S2, im S1, im S2 per eps order
+#if FT_PREC == 1
+    float Sf[4 * FT_K], Cf[4 * FT_K];   // FP32 Kahan sums, folded into S every 64 samples
+    int since_fold;
+    float keptf, droppedf, queuedf, exactf;   // counters below 2^24 between folds
+#endif
+    double kept, dropped, queued, exact, robust;
+
+    __device__ __forceinline__ void init()
+    {
+#pragma unroll
+        for (int s = 0; s < 4 * FT_K; s++) {
+            S[s].s = S[s].c = 0.0;
+#if FT_PREC == 1
+            Sf[s] = Cf[s] = 0.0f;
+#endif
+        }
+#if FT_PREC == 1
+        since_fold = 0;
+        keptf = droppedf = queuedf = exactf = 0.0f;
+#endif
+        kept = dropped = queued = exact = robust = 0.0;
+    }
+
+    __device__ __forceinline__ void add64(const cx<double>* R)
+    {
+        kept += 1;
+#pragma unroll
+        for (int j = 0; j < FT_K; j++) {
+            if (FT_ONLY_PSI && j > 0) break;
+            S[4 * j + 0].add(R[j].re);
+            S[4 * j + 1].add(R[j].re * R[j].re);
+            S[4 * j + 2].add(R[j].im);
+            S[4 * j + 3].add(R[j].im * R[j].im);
+        }
+    }
+
+#if FT_PREC == 1
+    __device__ __forceinline__ void add32(const cx<float>* R)
+    {
+        keptf += 1.0f;
+#pragma unroll
+        for (int j = 0; j < FT_K; j++) {
+            if (FT_ONLY_PSI && j > 0) break;
+            const float re = R[j].re, im = R[j].im;
+            const float v[4] = {re, re * re, im, im * im};
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const float y = v[q] - Cf[4 * j + q];
+                const float tt = Sf[4 * j + q] + y;
+                Cf[4 * j + q] = (tt - Sf[4 * j + q]) - y;
+                Sf[4 * j + q] = tt;
+            }
+        }
+        if (++since_fold == 256) fold();
+    }
+    __device__ __forceinline__ void note32(float d, float q, float e)
+    {
+        droppedf += d;
+        queuedf += q;
+        exactf += e;
+    }
+    __device__ __forceinline__ void fold()
+    {
+        since_fold = 0;
+#pragma unroll
+        for (int s = 0; s < 4 * FT_K; s++) {
+            S[s].add((double)Sf[s] - (double)Cf[s]);
+            Sf[s] = Cf[s] = 0.0f;
+        }
+        kept += keptf;
+        dropped += droppedf;
+        queued += queuedf;
+        exact += exactf;
+        keptf = droppedf = queuedf = exactf = 0.0f;
+    }
+#endif
+
+    __device__ __forceinline__ void finish(double* acc_out)
+    {
+#if FT_PREC == 1
+        fold();
+#endif
+        double vals[ACC_SLOTS];
+#pragma unroll
+        for (int s = 0; s < 4 * FT_K; s++) {
+            const double h = S[s].s + S[s].c;
+            vals[2 * s] = h;
+            vals[2 * s + 1] = S[s].c - (h - S[s].s);
+        }
+        vals[ACC_KEPT] = kept;
+        vals[ACC_DROPPED] = dropped;
+        vals[ACC_QUEUED] = queued;
+        vals[ACC_EXACT] = exact;
+        vals[ACC_ROBUST] = robust;
+#pragma unroll
+        for (int s = ACC_ROBUST + 1; s < ACC_SLOTS; s++) vals[s] = 0.0;
+        block_reduce(vals, acc_out);
+    }
+};
+
+template <class T>
+static __device__ __forceinline__ void write_record(u64 i, const unsigned char* ord, const cx<T>* R, bool ok,
+                                                    unsigned char flags, unsigned char* rec_order, double* rec_R,
+                                                    unsigned char* rec_flags)
+{
+    for (int e = 0; e < FT_E; e++) rec_order[i * FT_E + e] = ord[e];
+    for (int j = 0; j < FT_K; j++) {
+        rec_R[(i * FT_K + j) * 2] = ok ? (double)R[j].re : 0.0;
+        rec_R[(i * FT_K + j) * 2 + 1] = ok ? (double)R[j].im : 0.0;
+    }
+    rec_flags[i] = flags;
+}
+
+#if FT_PREC == 0
+// one sample in FP64 from stream state g (advanced past the sample's 2E-1 draws)
+static __device__ __forceinline__ void sample64(xo& g, const table_ref& tr, const double* prm, u64 i, accum& A,
+                                                unsigned char flags, unsigned char* rec_order, double* rec_X,
+                                                double* rec_R, unsigned char* rec_flags)
+{
+    unsigned char ord[FT_E];
+    cx<double> R[FT_K];
+#pragma unroll
+    for (int j = 0; j < FT_K; j++) R[j] = cmk(0.0, 0.0);
+    double X[FT_E];
+    double F, Gv;
+    draw_sector64(g, tr, prm[P_JRFULL], X, F, Gv, ord);
+    if (FT_RECORD)
+        for (int e = 0; e < FT_E; e++) rec_X[i * FT_E + e] = X[e];
+    bool rob = false;
+    const bool ok = integrand64(prm, X, F, Gv * F, R, rob);
+    if (rob) {
+        A.robust += 1;
+        flags |= REC_ROBUST;
+    }
+    if (!ok) {
+        A.dropped += 1;
+        flags |= REC_DROPPED;
+    } else {
+        A.add64(R);
+    }
+    if (FT_RECORD) write_record(i, ord, R, ok, flags, rec_order, rec_R, rec_flags);
+}
+#endif
+
+// ------------------------------------------------------------------ main kernel
+// Thread t of the launch owns samples [t*chunk, min(nsamples, (t+1)*chunk)) counted
+// from the launch's first sample, whose stream state is (s0..s3).  Block b writes
+// its partial sums to acc_out[b * ACC_SLOTS ...].  In the mixed form, samples whose
+// FP32 evaluation is not trustworthy are appended to `queue` (index and stream
+// state, 5 words) for the FP64 pass and left out of the sums here.
+extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample(
+    const double* __restrict__ prm, const unsigned char* __restrict__ tab, const u64* __restrict__ lanepw,
+    int lanebits, u64 s0, u64 s1, u64 s2, u64 s3, u64 nsamples, u64 chunk, double* __restrict__ acc_out,
+    u64* __restrict__ queue, unsigned int* __restrict__ qcount, unsigned int qcap,
+    unsigned char* __restrict__ rec_order, double* __restrict__ rec_X, double* __restrict__ rec_R,
+    unsigned char* __restrict__ rec_flags)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const table_ref tr = stage_table(smem, tab);
+
+    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+#if FT_PREC == 1
+    const float* pf = (const float*)(prm + P_SIZE);
+#endif
+    xo g;
+    g.a = s0;
+    g.b = s1;
+    g.c = s2;
+    g.d = s3;
+    skip_lanes(g, t, lanepw, lanebits);
+
+    u64 first = (u64)t * chunk;
+    u64 last = first + chunk;
+    if (last > nsamples) last = nsamples;
+
+    accum A;
+    A.init();
+    for (u64 i = first; i < last; i++) {
+#if FT_PREC == 0
+        sample64(g, tr, prm, i, A, 0, rec_order, rec_X, rec_R, rec_flags);
+#else
+        unsigned char ord[FT_E];
+        unsigned char flags = 0;
+        cx<float> R[FT_K];
+#pragma unroll
+        for (int j = 0; j < FT_K; j++) R[j] = cmk(0.0f, 0.0f);
+        const xo g0 = g;
+        f2 lx[FT_E], lF, lG;
+        const int ex = draw_sector32(g, tr, pf, lx, lF, lG, ord);
+        if (ex) flags |= REC_EXACT;
+        if (FT_RECORD)
+            for (int e = 0; e < FT_E; e++) rec_X[i * FT_E + e] = exp((double)lx[e].hi + (double)lx[e].lo);
+        bool need64 = false;
+        const bool ok = integrand32(pf, lx, lF, lG, R, need64);
+        if (need64) {
+            flags |= REC_QUEUED;
+            A.note32(0.0f, 1.0f, (float)ex);
+            const unsigned int slot = atomicAdd(qcount, 1u);
+            if (slot < qcap) {
+                u64* q = queue + (size_t)slot * 5;
+                q[0] = i;
+                q[1] = g0.a;
+                q[2] = g0.b;
+                q[3] = g0.c;
+                q[4] = g0.d;
+            }
+            if (FT_RECORD) write_record(i, ord, R, false, flags, rec_order, rec_R, rec_flags);
+            continue;
+        }
+        if (!ok) {
+            A.note32(1.0f, 0.0f, (float)ex);
+            flags |= REC_DROPPED;
+        } else {
+            A.note32(0.0f, 0.0f, (float)ex);
+            A.add32(R);
+        }
+        if (FT_RECORD) write_record(i, ord, R, ok, flags, rec_order, rec_R, rec_flags);
+#endif
+    }
+    A.finish(acc_out);
+}
+
+#if FT_PREC == 0
+// FP64 pass over the samples a mixed launch queued (grid-stride over the entries).
+extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue(
+    const double* __restrict__ prm, const unsigned char* __restrict__ tab, const u64* __restrict__ queue,
+    const unsigned int* __restrict__ qcount, unsigned int qcap, double* __restrict__ acc_out,
+    unsigned char* __restrict__ rec_order, double* __restrict__ rec_X, double* __restrict__ rec_R,
+    unsigned char* __restrict__ rec_flags)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const table_ref tr = stage_table(smem, tab);
+    unsigned int n = *qcount;
+    if (n > qcap) n = qcap;
+    accum A;
+    A.init();
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const u64* q = queue + (size_t)k * 5;
+        xo g;
+        g.a = q[1];
+        g.b = q[2];
+        g.c = q[3];
+        g.d = q[4];
+        sample64(g, tr, prm, q[0], A, REC_QUEUED, rec_order, rec_X, rec_R, rec_flags);
+    }
+    A.finish(acc_out);
+}
+#endif

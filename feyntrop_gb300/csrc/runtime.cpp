@@ -1,0 +1,655 @@
+// Plans, launches and the C ABI (include/feyntrop_gb300.h).
+//
+// A plan holds one integral: the host preprocessing result, its parameter block
+// and J(gamma) table in device memory, and the scratch its launches reuse.  An
+// integration is
+//   1. skip matrices for the launch's lane stride (cached per stride),
+//   2. the sampling kernel (one thread per contiguous block of samples),
+//   3. in mixed precision, the FP64 pass over the samples the FP32 kernel queued,
+//   4. the reduction of the per-block partial moments and one 512-byte copy back,
+// all on one stream.
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/feyntrop_gb300.h"
+#include "jit.hpp"
+#include "json.hpp"
+#include "kernels/aot.hpp"
+#include "problem.hpp"
+#include "xoshiro.hpp"
+
+namespace {
+
+thread_local std::string g_error;
+
+struct cuda_error : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+void cu(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw cuda_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int status_of(const std::exception_ptr& ep)
+{
+    try {
+        std::rethrow_exception(ep);
+    } catch (const std::invalid_argument& e) {
+        g_error = e.what();
+        return FT_ERR_INVALID_ARGUMENT;
+    } catch (const std::domain_error& e) {
+        g_error = e.what();
+        return FT_ERR_DOMAIN;
+    } catch (const cuda_error& e) {
+        g_error = e.what();
+        return FT_ERR_CUDA;
+    } catch (const std::runtime_error& e) {
+        g_error = e.what();
+        return FT_ERR_RUNTIME;
+    } catch (const std::exception& e) {
+        g_error = e.what();
+        return FT_ERR_RUNTIME;
+    } catch (...) {
+        g_error = "unknown error";
+        return FT_ERR_RUNTIME;
+    }
+}
+
+void require_device()
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n < 1) {
+        cudaGetLastError();
+        throw std::logic_error("no CUDA device: the feyntrop_gb300 sampling path runs on the GPU only");
+    }
+}
+
+// per-device constants: the 64 skip matrices T^(2^b)
+struct device_state {
+    unsigned long long* tpow = nullptr;
+    int sms = 0;
+};
+
+device_state& dev_state()
+{
+    static std::mutex mu;
+    static device_state st[64];
+    int dev = 0;
+    cu(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lock(mu);
+    device_state& d = st[dev & 63];
+    if (!d.tpow) {
+        const std::vector<uint64_t>& P = ft::power_table();
+        cu(cudaMalloc(&d.tpow, P.size() * 8), "cudaMalloc(skip matrices)");
+        cu(cudaMemcpy(d.tpow, P.data(), P.size() * 8, cudaMemcpyHostToDevice), "cudaMemcpy(skip matrices)");
+        cu(cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+    }
+    return d;
+}
+
+// P~ = P restricted to vertices 0..V-2 (vertex V-1 is the deleted one), split as
+// sum_r sigma_r q_r q_r^T; eigenpairs with |sigma| <= 1e-14 max|sigma| are dropped
+void low_rank(const ft::prepared& p, std::vector<double>& sigma, std::vector<double>& q)
+{
+    const int n = p.V - 1;
+    std::vector<double> A((size_t)n * n), Vv((size_t)n * n, 0.0);
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < n; j++) A[i * n + j] = p.P[i * p.V + j];
+    for (int i = 0; i < n; i++) Vv[i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 100; sweep++) {
+        double off = 0;
+        for (int i = 0; i < n; i++)
+            for (int j = i + 1; j < n; j++) off += A[i * n + j] * A[i * n + j];
+        if (off < 1e-300) break;
+        for (int a = 0; a < n; a++)
+            for (int b = a + 1; b < n; b++) {
+                double apq = A[a * n + b];
+                if (apq == 0.0) continue;
+                double theta = (A[b * n + b] - A[a * n + a]) / (2.0 * apq);
+                double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
+                for (int k = 0; k < n; k++) {
+                    double akp = A[k * n + a], akq = A[k * n + b];
+                    A[k * n + a] = c * akp - s * akq;
+                    A[k * n + b] = s * akp + c * akq;
+                }
+                for (int k = 0; k < n; k++) {
+                    double apk = A[a * n + k], aqk = A[b * n + k];
+                    A[a * n + k] = c * apk - s * aqk;
+                    A[b * n + k] = s * apk + c * aqk;
+                }
+                for (int k = 0; k < n; k++) {
+                    double vka = Vv[k * n + a], vkb = Vv[k * n + b];
+                    Vv[k * n + a] = c * vka - s * vkb;
+                    Vv[k * n + b] = s * vka + c * vkb;
+                }
+            }
+    }
+    double mx = 0;
+    for (int i = 0; i < n; i++) mx = std::max(mx, std::fabs(A[i * n + i]));
+    sigma.clear();
+    q.clear();
+    for (int r = 0; r < n; r++) {
+        double ev = A[r * n + r];
+        if (mx == 0.0 || std::fabs(ev) <= 1e-14 * mx) continue;
+        sigma.push_back(ev);
+        for (int i = 0; i < n; i++) q.push_back(Vv[i * n + r]);
+    }
+    if (sigma.empty()) {   // P~ = 0: one zero term keeps the arrays non-empty
+        sigma.push_back(0.0);
+        q.assign(n, 0.0);
+    }
+}
+
+}  // namespace
+
+struct ft_plan {
+    ft::prepared P;
+    std::vector<double> sigma, q, prm;
+    std::vector<unsigned char> tab;
+    int device = 0;
+    double* d_prm = nullptr;
+    unsigned char* d_tab = nullptr;
+    // scratch reused by launches
+    double* d_parts = nullptr;
+    size_t parts_cap = 0;
+    double* d_final = nullptr;
+    double* h_final = nullptr;
+    unsigned long long* d_queue = nullptr;
+    unsigned int* d_qcount = nullptr;
+    size_t qcap = 0;
+    unsigned long long* d_lanepw = nullptr;
+    unsigned long long lanepw_S = 0;
+    int lanepw_bits = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::mutex mu;
+
+    ft::kernel_key key(int prec, int record) const
+    {
+        ft::kernel_key k;
+        k.E = P.E;
+        k.V = P.V;
+        k.K = P.K;
+        k.loops = P.loops;
+        k.rank = (int)sigma.size();
+        k.prec = prec;
+        k.mode = P.deformed() ? 1 : 0;
+        k.only_psi = P.only_psi() ? 1 : 0;
+        k.record = record;
+        k.block = 128;
+        k.ek = P.ek;
+        k.el = P.el;
+        // stage the table in shared memory when it fits comfortably
+        const size_t bytes = (size_t)(prec == 0 ? 25 : 13) << P.E;
+        k.table_global = bytes > 160 * 1024 ? 1 : 0;
+        return k;
+    }
+
+    int slots() const { return 8 * P.K + 8; }
+
+    ~ft_plan()
+    {
+        if (d_prm) cudaFree(d_prm);
+        if (d_tab) cudaFree(d_tab);
+        if (d_parts) cudaFree(d_parts);
+        if (d_final) cudaFree(d_final);
+        if (h_final) cudaFreeHost(h_final);
+        if (d_queue) cudaFree(d_queue);
+        if (d_qcount) cudaFree(d_qcount);
+        if (d_lanepw) cudaFree(d_lanepw);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+// parameter block and table bytes in the layout the kernel body expects
+void build_blocks(ft_plan& pl)
+{
+    const ft::prepared& p = pl.P;
+    const int E = p.E, n = p.V - 1, R = (int)pl.sigma.size();
+    pl.prm.assign(8 + 2 * E + R + R * n, 0.0);
+    pl.prm[0] = p.D;
+    pl.prm[1] = p.W;
+    pl.prm[2] = p.IGtr;
+    pl.prm[3] = p.def_ref;
+    pl.prm[4] = 1. / (p.D / 2. * p.loops + p.W);
+    pl.prm[5] = p.Jr[(1ULL << E) - 1];
+    for (int e = 0; e < E; e++) {
+        pl.prm[8 + e] = p.m2[e];
+        pl.prm[8 + E + e] = p.nu[e];
+    }
+    for (int r = 0; r < R; r++) {
+        pl.prm[8 + 2 * E + r] = pl.sigma[r];
+        for (int i = 0; i < n; i++) pl.prm[8 + 2 * E + R + r * n + i] = pl.q[r * n + i];
+    }
+    const size_t N = 1ULL << E;
+    const size_t f32 = (25 * N + 15) & ~(size_t)15;
+    pl.tab.assign(f32 + 12 * N, 0);
+    double* w64 = (double*)pl.tab.data();
+    double* Jr64 = w64 + N;
+    double* ri64 = w64 + 2 * N;
+    unsigned char* meta = pl.tab.data() + 24 * N;
+    float* w32 = (float*)(pl.tab.data() + f32);
+    float* Jr32 = w32 + N;
+    float* ri32 = w32 + 2 * N;
+    for (size_t s = 0; s < N; s++) {
+        // the scan adds Jr/r and the X update raises to 1./r (srcs/tropical_sampling.hpp:487,558)
+        w64[s] = p.Jr[s] / p.r[s];
+        Jr64[s] = p.Jr[s];
+        ri64[s] = 1. / p.r[s];
+        meta[s] = (unsigned char)((p.mm[s] ? 0x80 : 0) | (p.L[s] & 0x7f));
+        w32[s] = (float)w64[s];
+        Jr32[s] = (float)Jr64[s];
+        ri32[s] = (float)ri64[s];
+    }
+}
+
+void upload(ft_plan& pl)
+{
+    cu(cudaGetDevice(&pl.device), "cudaGetDevice");
+    // FP64 parameter block followed by the same values as floats
+    std::vector<double> blk(pl.prm.size() + (pl.prm.size() + 1) / 2, 0.0);
+    std::memcpy(blk.data(), pl.prm.data(), pl.prm.size() * 8);
+    float* f = (float*)(blk.data() + pl.prm.size());
+    for (size_t i = 0; i < pl.prm.size(); i++) f[i] = (float)pl.prm[i];
+    cu(cudaMalloc(&pl.d_prm, blk.size() * 8), "cudaMalloc(params)");
+    cu(cudaMalloc(&pl.d_tab, pl.tab.size()), "cudaMalloc(table)");
+    cu(cudaMemcpy(pl.d_prm, blk.data(), blk.size() * 8, cudaMemcpyHostToDevice), "cudaMemcpy(params)");
+    cu(cudaMemcpy(pl.d_tab, pl.tab.data(), pl.tab.size(), cudaMemcpyHostToDevice), "cudaMemcpy(table)");
+    cu(cudaStreamCreateWithFlags(&pl.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    cu(cudaEventCreate(&pl.ev0), "cudaEventCreate");
+    cu(cudaEventCreate(&pl.ev1), "cudaEventCreate");
+    cu(cudaMalloc(&pl.d_final, pl.slots() * 8), "cudaMalloc(final)");
+    cu(cudaMallocHost(&pl.h_final, pl.slots() * 8), "cudaMallocHost(final)");
+    cu(cudaMalloc(&pl.d_qcount, 16), "cudaMalloc(queue count)");
+}
+
+void ensure_parts(ft_plan& pl, size_t nparts)
+{
+    size_t need = nparts * pl.slots();
+    if (need <= pl.parts_cap) return;
+    if (pl.d_parts) cudaFree(pl.d_parts);
+    pl.d_parts = nullptr;
+    cu(cudaMalloc(&pl.d_parts, need * 8), "cudaMalloc(partial sums)");
+    pl.parts_cap = need;
+}
+
+void ensure_queue(ft_plan& pl, size_t entries)
+{
+    if (entries <= pl.qcap) return;
+    if (pl.d_queue) cudaFree(pl.d_queue);
+    pl.d_queue = nullptr;
+    cu(cudaMalloc(&pl.d_queue, entries * 5 * 8), "cudaMalloc(FP64 queue)");
+    pl.qcap = entries;
+}
+
+void ensure_lanepw(ft_plan& pl, unsigned long long S, int bits, cudaStream_t st)
+{
+    if (pl.d_lanepw && pl.lanepw_S == S && pl.lanepw_bits >= bits) return;
+    if (!pl.d_lanepw) cu(cudaMalloc(&pl.d_lanepw, (size_t)64 * 1024 * 8), "cudaMalloc(lane skip matrices)");
+    cu(ft::launch_lane_powers(dev_state().tpow, S, bits, pl.d_lanepw, st), "lane skip matrices");
+    pl.lanepw_S = S;
+    pl.lanepw_bits = bits;
+}
+
+struct launch_geometry {
+    unsigned blocks;
+    unsigned long long chunk;
+    int lanebits;
+};
+
+launch_geometry geometry(const ft::kernel_set& ks, unsigned long long N)
+{
+    const unsigned long long max_threads = (unsigned long long)dev_state().sms * ks.blocks_per_sm * ks.block;
+    launch_geometry g;
+    g.chunk = N == 0 ? 1 : (N + max_threads - 1) / max_threads;
+    const unsigned long long threads = N == 0 ? 1 : (N + g.chunk - 1) / g.chunk;
+    g.blocks = (unsigned)((threads + ks.block - 1) / ks.block);
+    g.lanebits = 1;
+    while ((1ULL << g.lanebits) < (unsigned long long)g.blocks * ks.block) g.lanebits++;
+    return g;
+}
+
+struct records {
+    uint8_t* order = nullptr;
+    double* X = nullptr;
+    double* R = nullptr;
+    uint8_t* flags = nullptr;
+};
+
+struct run_out {
+    std::vector<double> acc;   // slots
+    double kernel_ms = 0;
+    int launches = 0;
+};
+
+// the launches of one integration (or one record run) on stream st
+run_out run(ft_plan& pl, const ft_run_options& o, cudaStream_t st, const records* rec)
+{
+    const int prec = o.precision == FT_PRECISION_MIXED ? 1 : 0;
+    const int record = rec ? 1 : 0;
+    const ft::kernel_set& ks = ft::get_kernels(pl.key(prec, record));
+    const ft::kernel_set* k64 = prec ? &ft::get_kernels(pl.key(0, record)) : nullptr;
+    const unsigned long long N = o.num_samples;
+    const launch_geometry g = geometry(ks, N);
+    const unsigned long long draws = 2ULL * pl.P.E - 1;
+    run_out out;
+    out.acc.assign(pl.slots(), 0.0);
+    if (N == 0) return out;
+
+    ensure_lanepw(pl, g.chunk * draws, g.lanebits, st);
+    out.launches++;
+    const unsigned qblocks = prec ? (unsigned)(dev_state().sms * std::max(1, k64->queue_blocks_per_sm)) : 0;
+    ensure_parts(pl, g.blocks + qblocks);
+    if (prec) {
+        size_t want = (size_t)std::min<unsigned long long>(N, N / 16 + 65536);
+        ensure_queue(pl, want);
+    }
+    cu(cudaMemsetAsync(pl.d_qcount, 0, 16, st), "cudaMemsetAsync");
+    const ft::xstate base = ft::advance(ft::seed_state(o.seed), o.first_sample * draws);
+
+    unsigned long long s0 = base.s[0], s1 = base.s[1], s2 = base.s[2], s3 = base.s[3];
+    unsigned long long nsamples = N, chunk = g.chunk;
+    int lanebits = g.lanebits;
+    unsigned int qcap = (unsigned int)pl.qcap;
+    unsigned long long* queue = pl.d_queue;
+    unsigned int* qcount = pl.d_qcount;
+    double* parts = pl.d_parts;
+    const double* prm = pl.d_prm;
+    const unsigned char* tab = pl.d_tab;
+    const unsigned long long* lanepw = pl.d_lanepw;
+    uint8_t* r_order = nullptr;
+    double* r_X = nullptr;
+    double* r_R = nullptr;
+    uint8_t* r_flags = nullptr;
+    if (rec) {
+        r_order = rec->order;
+        r_X = rec->X;
+        r_R = rec->R;
+        r_flags = rec->flags;
+    }
+    void* args[] = {&prm, &tab, &lanepw, &lanebits, &s0, &s1, &s2, &s3, &nsamples, &chunk, &parts, &queue, &qcount,
+                    &qcap, &r_order, &r_X, &r_R, &r_flags};
+    cu(cudaEventRecord(pl.ev0, st), "cudaEventRecord");
+    ft::check(ft::drv().LaunchKernel(ks.sample, g.blocks, 1, 1, ks.block, 1, 1, ks.smem, (CUstream)st, args, nullptr),
+              "launch ft_sample");
+    out.launches++;
+    if (prec) {
+        double* qparts = pl.d_parts + (size_t)g.blocks * pl.slots();
+        const unsigned long long* cq = pl.d_queue;
+        const unsigned int* cqc = pl.d_qcount;
+        void* qargs[] = {&prm, &tab, &cq, &cqc, &qcap, &qparts, &r_order, &r_X, &r_R, &r_flags};
+        ft::check(ft::drv().LaunchKernel(k64->queue, qblocks, 1, 1, k64->block, 1, 1, k64->smem, (CUstream)st, qargs,
+                                         nullptr),
+                  "launch ft_sample_queue");
+        out.launches++;
+    }
+    cu(cudaEventRecord(pl.ev1, st), "cudaEventRecord");
+    cu(ft::launch_finalize(pl.d_parts, (int)(g.blocks + qblocks), pl.slots(), 8 * pl.P.K, pl.d_final, st),
+       "finalize");
+    out.launches++;
+    cu(cudaMemcpyAsync(pl.h_final, pl.d_final, pl.slots() * 8, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+    unsigned int qc_host = 0;
+    if (prec) cu(cudaMemcpyAsync(&qc_host, pl.d_qcount, 4, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+    cu(cudaStreamSynchronize(st), "sampling");
+    float ms = 0;
+    cu(cudaEventElapsedTime(&ms, pl.ev0, pl.ev1), "cudaEventElapsedTime");
+    out.kernel_ms = ms;
+    out.acc.assign(pl.h_final, pl.h_final + pl.slots());
+    if (prec && qc_host > pl.qcap) {
+        // more samples needed FP64 than the queue holds: redo the whole range in FP64
+        ft_run_options o64 = o;
+        o64.precision = FT_PRECISION_FP64;
+        run_out r = run(pl, o64, st, rec);
+        r.acc[8 * pl.P.K + 2] = qc_host;
+        r.launches += out.launches;
+        r.kernel_ms += out.kernel_ms;
+        return r;
+    }
+    return out;
+}
+
+void fill_result(const ft::prepared& P, const std::vector<double>& acc, ft_result* r)
+{
+    const int K = P.K;
+    r->num_eps_terms = K;
+    r->kept = (uint64_t)acc[8 * K];
+    r->dropped = (uint64_t)acc[8 * K + 1];
+    r->fp64_fallback = (uint64_t)acc[8 * K + 2];
+    r->exact_steps = (uint64_t)acc[8 * K + 3];
+    r->robust = (uint64_t)acc[8 * K + 4];
+    std::vector<ft_moments> m(2 * K);
+    for (int j = 0; j < K; j++)
+        for (int part = 0; part < 2; part++) {
+            ft_moments& x = m[2 * j + part];
+            x.n = (double)r->kept;
+            x.s1_hi = acc[8 * j + 4 * part + 0];
+            x.s1_lo = acc[8 * j + 4 * part + 1];
+            x.s2_hi = acc[8 * j + 4 * part + 2];
+            x.s2_lo = acc[8 * j + 4 * part + 3];
+        }
+    if (r->moments) std::memcpy(r->moments, m.data(), m.size() * sizeof(ft_moments));
+    ft_finalize_moments(m.data(), K, P.deformed() ? 0 : 1, r);
+}
+
+}  // namespace
+
+static ft::problem_input input_of(const ft_problem* pb)
+{
+    if (!pb || pb->num_edges < 1 || !pb->edges || !pb->nu || !pb->masses_sqr || !pb->scalarproducts)
+        throw std::invalid_argument("empty or incomplete problem");
+    ft::problem_input in;
+    int Vmax = 0;
+    for (int e = 0; e < pb->num_edges; e++) {
+        in.v.push_back(pb->edges[2 * e]);
+        in.w.push_back(pb->edges[2 * e + 1]);
+        in.nu.push_back(pb->nu[e]);
+        in.m2.push_back(pb->masses_sqr[e]);
+        Vmax = std::max(Vmax, std::max(pb->edges[2 * e], pb->edges[2 * e + 1]) + 1);
+    }
+    const int V = pb->num_vertices >= 0 ? pb->num_vertices : Vmax;
+    if (V != Vmax) throw std::invalid_argument("input scalarproducts must be a (V x V)-matrix");
+    in.P.assign(pb->scalarproducts, pb->scalarproducts + (size_t)V * V);
+    in.D = pb->dimension;
+    in.K = pb->num_eps_terms;
+    in.lambda = pb->lambda;
+    if (in.K < 1) throw std::invalid_argument("num_eps_terms must be at least 1");
+    return in;
+}
+
+static void info_of(const ft::prepared& P, size_t table_bytes, ft_plan_info* info)
+{
+    info->W = P.W;
+    info->IGtr = P.IGtr;
+    info->loops = P.loops;
+    info->euclidean = P.euclidean;
+    info->pseudo_euclidean = P.pseudo_euclidean;
+    info->generic = P.generic;
+    info->gp_property = P.gp;
+    info->deformed = P.deformed();
+    info->lambda_used = P.lambda;
+    info->seconds_preprocessing = P.seconds_preprocessing;
+    info->table_bytes = table_bytes;
+    info->num_log_lines = (int)P.log.size();
+}
+
+// ------------------------------------------------------------------ C ABI
+extern "C" {
+
+const char* ft_last_error(void) { return g_error.c_str(); }
+const char* ft_version(void) { return "feyntrop_gb300 0.1 (sm_103a)"; }
+void ft_free(void* p) { std::free(p); }
+
+int ft_plan_create(const ft_problem* pb, ft_plan** out)
+{
+    *out = nullptr;
+    try {
+        ft::problem_input in = input_of(pb);
+        std::unique_ptr<ft_plan> pl(new ft_plan());
+        pl->P = ft::prepare(in);
+        if (pl->P.E > 24) throw std::domain_error("graphs with more than 24 edges are not supported by the GPU sampler");
+        require_device();
+        low_rank(pl->P, pl->sigma, pl->q);
+        build_blocks(*pl);
+        dev_state();
+        upload(*pl);
+        *out = pl.release();
+        return FT_OK;
+    } catch (const std::logic_error& e) {
+        if (dynamic_cast<const std::invalid_argument*>(&e) || dynamic_cast<const std::domain_error*>(&e))
+            return status_of(std::current_exception());
+        g_error = e.what();
+        return FT_ERR_NO_DEVICE;
+    } catch (...) {
+        return status_of(std::current_exception());
+    }
+}
+
+void ft_plan_destroy(ft_plan* p) { delete p; }
+
+int ft_plan_get_info(const ft_plan* pl, ft_plan_info* info)
+{
+    info_of(pl->P, pl->tab.size(), info);
+    return FT_OK;
+}
+
+const char* ft_plan_log_line(const ft_plan* pl, int32_t i)
+{
+    if (i < 0 || i >= (int)pl->P.log.size()) return "";
+    return pl->P.log[i].c_str();
+}
+
+int ft_subgraph_table(const ft_problem* pb, double* Jr, double* r, uint8_t* mm, uint8_t* L, ft_plan_info* info)
+{
+    try {
+        ft::prepared P = ft::prepare(input_of(pb));
+        const size_t n = P.Jr.size();
+        if (Jr) std::memcpy(Jr, P.Jr.data(), n * 8);
+        if (r) std::memcpy(r, P.r.data(), n * 8);
+        if (mm) std::memcpy(mm, P.mm.data(), n);
+        if (L) std::memcpy(L, P.L.data(), n);
+        if (info) info_of(P, 0, info);
+        return FT_OK;
+    } catch (...) {
+        return status_of(std::current_exception());
+    }
+}
+
+int ft_precompile(const ft_problem* pb, int32_t precision, double* seconds)
+{
+    try {
+        ft::problem_input in = input_of(pb);
+        ft_plan pl;
+        pl.P = ft::prepare(in);
+        low_rank(pl.P, pl.sigma, pl.q);
+        auto t0 = std::chrono::steady_clock::now();
+        ft::precompile(pl.key(0, 0));
+        if (precision == FT_PRECISION_MIXED) ft::precompile(pl.key(1, 0));
+        if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return FT_OK;
+    } catch (...) {
+        return status_of(std::current_exception());
+    }
+}
+
+int ft_finalize_moments(const ft_moments* m, int32_t K, int32_t real_only, ft_result* r)
+{
+    // srcs/stats.hpp:86-104 on the merged sums (long double for the final arithmetic)
+    for (int j = 0; j < K; j++) {
+        for (int part = 0; part < 2; part++) {
+            const ft_moments& x = m[2 * j + part];
+            double avg, acc;
+            if (part == 1 && real_only) {
+                avg = 0.0;   // two zero updates per thread in the reference (srcs/feynman_integral.hpp:130-140)
+                acc = 0.0;
+            } else {
+                const long double N = x.n;
+                const long double S1 = (long double)x.s1_hi + x.s1_lo, S2 = (long double)x.s2_hi + x.s2_lo;
+                const long double a = S1 / N;
+                const long double var = (N / (N - 1)) * (S2 / N - a * a);
+                avg = (double)a;
+                acc = (double)std::sqrt(var / N);
+            }
+            if (part == 0) {
+                if (r->re_avg) r->re_avg[j] = avg;
+                if (r->re_acc) r->re_acc[j] = acc;
+            } else {
+                if (r->im_avg) r->im_avg[j] = avg;
+                if (r->im_acc) r->im_acc[j] = acc;
+            }
+        }
+    }
+    return FT_OK;
+}
+
+int ft_integrate(ft_plan* pl, const ft_run_options* o, ft_result* r)
+{
+    try {
+        std::lock_guard<std::mutex> lock(pl->mu);
+        auto t0 = std::chrono::steady_clock::now();
+        cu(cudaSetDevice(pl->device), "cudaSetDevice");
+        cudaStream_t st = o->stream ? (cudaStream_t)o->stream : pl->stream;
+        run_out ro = run(*pl, *o, st, nullptr);
+        fill_result(pl->P, ro.acc, r);
+        r->kernel_ms = ro.kernel_ms;
+        r->kernel_launches = ro.launches;
+        r->seconds_sampling = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        return FT_OK;
+    } catch (...) {
+        return status_of(std::current_exception());
+    }
+}
+
+int ft_integrate_batch(ft_plan* const* plans, int32_t count, const ft_run_options* opts, ft_result* results)
+{
+    for (int i = 0; i < count; i++) {
+        int rc = ft_integrate(plans[i], &opts[i], &results[i]);
+        if (rc != FT_OK) return rc;
+    }
+    return FT_OK;
+}
+
+int ft_sample_records(ft_plan* pl, const ft_run_options* o, uint8_t* order, double* X, double* R, uint8_t* flags)
+{
+    try {
+        std::lock_guard<std::mutex> lock(pl->mu);
+        cu(cudaSetDevice(pl->device), "cudaSetDevice");
+        const size_t N = o->num_samples, E = pl->P.E, K = pl->P.K;
+        records d;
+        cu(cudaMalloc(&d.order, N * E + 1), "cudaMalloc(records)");
+        cu(cudaMalloc(&d.X, N * E * 8 + 8), "cudaMalloc(records)");
+        cu(cudaMalloc(&d.R, N * K * 16 + 16), "cudaMalloc(records)");
+        cu(cudaMalloc(&d.flags, N + 1), "cudaMalloc(records)");
+        cu(cudaMemset(d.flags, 0, N + 1), "cudaMemset");
+        run(*pl, *o, pl->stream, &d);
+        if (order) cu(cudaMemcpy(order, d.order, N * E, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        if (X) cu(cudaMemcpy(X, d.X, N * E * 8, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        if (R) cu(cudaMemcpy(R, d.R, N * K * 16, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        if (flags) cu(cudaMemcpy(flags, d.flags, N, cudaMemcpyDeviceToHost), "cudaMemcpy");
+        cudaFree(d.order);
+        cudaFree(d.X);
+        cudaFree(d.R);
+        cudaFree(d.flags);
+        return FT_OK;
+    } catch (...) {
+        return status_of(std::current_exception());
+    }
+}
+
+}  // extern "C"

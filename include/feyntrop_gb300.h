@@ -1,0 +1,149 @@
+/*
+ * feyntrop_gb300 — C ABI of the GB300 tropical sampling + integrand evaluation path.
+ *
+ * This library replaces the reference's in-process seam
+ *
+ *   generate_subgraph_table(g, D, P, m2, eps_expansion, bNonEuclidean)
+ *       srcs/tropical_sampling.hpp:284-291
+ *   feynman_integral_estimate(N, g, D, P, m2, num_eps_terms, lambda, table, gen)
+ *       srcs/feynman_integral.hpp:30-41, called from srcs/feyntrop.cpp:251
+ *
+ * and the decisions the CLI makes around it (srcs/feyntrop.cpp:25-239).  Plain
+ * pointers and sizes only; no exception crosses the boundary: every call returns
+ * a status code and ft_last_error() holds the reference's message for the last
+ * failure on the calling thread.  Caller-owned result buffers.  Distinct plans may
+ * be used from different host threads concurrently.
+ */
+#ifndef FEYNTROP_GB300_H
+#define FEYNTROP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; the reference throws the matching C++ exception type */
+#define FT_OK 0
+#define FT_ERR_INVALID_ARGUMENT 1 /* std::invalid_argument (input shape, graph checks) */
+#define FT_ERR_DOMAIN 2           /* std::domain_error (kinematics, divergences, GP checks) */
+#define FT_ERR_RUNTIME 3          /* std::runtime_error */
+#define FT_ERR_CUDA 4             /* device, driver or runtime-compiler failure */
+#define FT_ERR_NO_DEVICE 5        /* no CUDA device: this library has no CPU path */
+
+/* arithmetic of the sampling kernels */
+#define FT_PRECISION_FP64 0  /* every operation in FP64 */
+#define FT_PRECISION_MIXED 1 /* FP32 integrand, FP64 sector decisions, FP64 re-evaluation of flagged samples */
+
+typedef struct ft_plan ft_plan;
+
+/* One Feynman integral: the reference's low-level JSON input as arrays
+ * (srcs/feyntrop.cpp:39-96). */
+typedef struct {
+    int32_t num_edges;            /* E */
+    const int32_t* edges;         /* 2E vertex numbers, edge e = (edges[2e], edges[2e+1]) */
+    const double* nu;             /* E edge weights */
+    int32_t num_vertices;         /* V; must equal max vertex + 1, or -1 to derive it */
+    const double* scalarproducts; /* V*V, row major */
+    const double* masses_sqr;     /* E */
+    double dimension;             /* D */
+    int32_t num_eps_terms;        /* K >= 1 */
+    double lambda;                /* deformation parameter */
+} ft_problem;
+
+/* Host preprocessing and upload: input checks, regime decision and the J(gamma)
+ * table (replaces srcs/feyntrop.cpp:64-239 and generate_subgraph_table). */
+int ft_plan_create(const ft_problem* problem, ft_plan** out);
+void ft_plan_destroy(ft_plan* plan);
+
+typedef struct {
+    double W;                     /* superficial degree of divergence */
+    double IGtr;                  /* tropical normalisation I_G^tr */
+    int32_t loops;
+    int32_t euclidean, pseudo_euclidean, generic, gp_property;
+    int32_t deformed;             /* 1 when the contour deformation is used */
+    double lambda_used;
+    double seconds_preprocessing;
+    uint64_t table_bytes;         /* device bytes of the J(gamma) table */
+    int32_t num_log_lines;        /* diagnostics the reference prints to stderr */
+} ft_plan_info;
+
+int ft_plan_get_info(const ft_plan* plan, ft_plan_info* info);
+/* i-th diagnostic line (0-based), NUL-terminated, owned by the plan */
+const char* ft_plan_log_line(const ft_plan* plan, int32_t i);
+
+typedef struct {
+    uint64_t num_samples;   /* N */
+    uint64_t seed;
+    uint64_t first_sample;  /* index of the first sample in the seed's stream (sharding) */
+    int32_t precision;      /* FT_PRECISION_* */
+    void* stream;           /* cudaStream_t, NULL for the library's own stream */
+} ft_run_options;
+
+/* Raw sums, mergeable across shards: per eps order j and part p (0 = Re, 1 = Im)
+ * the slot [2j+p] holds count, sum f (hi, lo) and sum f^2 (hi, lo). */
+typedef struct {
+    double n;
+    double s1_hi, s1_lo, s2_hi, s2_lo;
+} ft_moments;
+
+typedef struct {
+    int32_t num_eps_terms;    /* K, entries in the arrays below */
+    double* re_avg;           /* caller-owned, K each */
+    double* re_acc;
+    double* im_avg;
+    double* im_acc;
+    ft_moments* moments;      /* caller-owned 2K entries, may be NULL */
+    uint64_t kept, dropped;   /* samples accumulated / dropped as non-finite */
+    uint64_t fp64_fallback;   /* mixed: samples re-evaluated in FP64 */
+    uint64_t exact_steps;     /* mixed: sector steps decided by the FP64 re-check */
+    uint64_t robust;          /* complex Laplacians that needed complete pivoting */
+    double kernel_ms;         /* device time of the sampling kernels (CUDA events) */
+    double seconds_sampling;  /* host wall time of the call */
+    int32_t kernel_launches;
+} ft_result;
+
+/* Samples first_sample .. first_sample+N-1 of the seed's stream (replaces
+ * feynman_integral_estimate).  With first_sample = 0 the samples are exactly those
+ * of the reference run with OMP_NUM_THREADS=1. */
+int ft_integrate(ft_plan* plan, const ft_run_options* opts, ft_result* result);
+
+/* Several plans in one call (one launch per plan today, all on one stream). */
+int ft_integrate_batch(ft_plan* const* plans, int32_t count, const ft_run_options* opts, ft_result* results);
+
+/* avg / acc from merged moments, with the reference's formulas (srcs/stats.hpp:86-104);
+ * real_only marks integrals whose imaginary part the reference reports as (0, 0). */
+int ft_finalize_moments(const ft_moments* moments, int32_t num_eps_terms, int32_t real_only, ft_result* result);
+
+/* Per-sample records of samples first_sample .. +N-1 (parity checks): removal order
+ * (N x E bytes), X before rescaling (N x E), integrand per eps order (N x K x 2:
+ * re, im) and flags (bit 0 dropped, 1 re-evaluated in FP64, 2 exact sector step,
+ * 3 complete-pivoting LU).  Any pointer may be NULL. */
+int ft_sample_records(ft_plan* plan, const ft_run_options* opts, uint8_t* order, double* X, double* R,
+                      uint8_t* flags);
+
+/* The reference's CLI contract in process: input JSON text in, output JSON text
+ * out (srcs/feyntrop.cpp:20-281).  *output is malloc'd; free with ft_free. */
+int ft_run_json(const char* input_json, char** output, char** log);
+void ft_free(void* p);
+
+/* Host preprocessing only (no device): the J(gamma) table of
+ * generate_subgraph_table (srcs/tropical_sampling.hpp:284-458), indexed by the edge
+ * bitmask of gamma, 2^E entries each (Jr, r, mass-momentum-spanning flag, loop
+ * number), and the plan information.  Any output pointer may be NULL. */
+int ft_subgraph_table(const ft_problem* problem, double* Jr, double* r, uint8_t* mm, uint8_t* loops,
+                      ft_plan_info* info);
+
+/* Host preprocessing plus run-time compilation of the sampling kernels for this
+ * problem's topology (FP64 and, if requested, mixed), without touching a device:
+ * warms the kernel cache.  *seconds receives the compile time (0 when cached). */
+int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds);
+
+const char* ft_last_error(void);
+const char* ft_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,136 @@
+"""GPU path against the oracle and the reference's outputs (all through the C ABI).
+
+Same samples as the reference's single-thread run: the GPU walks the seed's single
+xoshiro256+ stream, so sector orders must be bit-identical and per-sample values
+agree to FP64 rounding (plain FP64 form) or to the stated mixed-precision
+tolerance; integrals over the same samples then agree far inside the statistical
+error, and the reference's own test-suite expectations hold within 4 combined
+standard errors.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import feyntrop_gb300 as ft
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+PINS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_pins.json")))
+CASES = sorted(PINS["cases"])
+N_REC = 4096
+
+# per-sample relative error, |R_gpu - R_oracle| / max_j |R_oracle_j| of the sample
+FP64_MEDIAN_TOL = 1e-12
+FP64_MAX_TOL = 1e-7      # ill-conditioned sectors: both are FP64 solutions of the same system
+MIXED_P999_TOL = 1e-5    # 99.9 % of the samples
+MIXED_MAX_TOL = 1e-3
+
+_plans = {}
+
+
+def plan(name):
+    if name not in _plans:
+        _plans[name] = ft.Plan(PINS["cases"][name]["input"])
+    return _plans[name]
+
+
+def sample_errors(rec, ref):
+    ok = ~ref["dropped"]
+    scale = np.abs(ref["R"]).max(axis=1)
+    err = np.abs(rec["R"] - ref["R"]).max(axis=1) / np.where(scale > 0, scale, 1.0)
+    return err[ok]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fp64_samples_match_oracle(name):
+    p = plan(name)
+    ref = ol.Prepared(PINS["cases"][name]["input"]).samples(0, 0, N_REC)
+    rec = p.records(N_REC, seed=0, precision=ft.FP64)
+    assert (rec["order"] == ref["order"]).all(), "sector orders differ"
+    assert np.allclose(rec["X"], ref["X"], rtol=1e-13, atol=0)
+    assert ((rec["flags"] & 1).astype(bool) == ref["dropped"]).all()
+    err = sample_errors(rec, ref)
+    print(name, "fp64 per-sample rel err: median %.2e p99.9 %.2e max %.2e" % (
+        np.median(err), np.quantile(err, 0.999), err.max()))
+    assert np.median(err) < FP64_MEDIAN_TOL
+    assert err.max() < FP64_MAX_TOL
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_mixed_samples_match_oracle(name):
+    p = plan(name)
+    ref = ol.Prepared(PINS["cases"][name]["input"]).samples(0, 0, N_REC)
+    rec = p.records(N_REC, seed=0, precision=ft.MIXED)
+    assert (rec["order"] == ref["order"]).all(), "sector orders differ"
+    err = sample_errors(rec, ref)
+    queued = (rec["flags"] & 2).astype(bool).mean()
+    print(name, "mixed per-sample rel err: median %.2e p99.9 %.2e max %.2e; FP64 re-evaluated %.4f" % (
+        np.median(err), np.quantile(err, 0.999), err.max(), queued))
+    assert np.quantile(err, 0.999) < MIXED_P999_TOL
+    assert err.max() < MIXED_MAX_TOL
+
+
+def test_skip_ahead_matches_stream_order():
+    name = "C2_double_box"
+    p = plan(name)
+    a = p.records(600, seed=5, first_sample=0)
+    b = p.records(100, seed=5, first_sample=500)
+    assert (a["order"][500:] == b["order"]).all()
+    assert (a["X"][500:] == b["X"]).all()
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_integral_same_samples_as_reference(name):
+    c = PINS["cases"][name]
+    p = plan(name)
+    N = PINS["N_aggregate"]
+    r64 = p.integrate(N, seed=0, precision=ft.FP64)
+    rmx = p.integrate(N, seed=0, precision=ft.MIXED)
+    for j, ((re, dre), (im, dim)) in enumerate(c["aggregate"]["integral"]):
+        g_re, g_dre = r64["integral"][j][0]
+        g_im, g_dim = r64["integral"][j][1]
+        # identical samples: differences are rounding only
+        assert abs(g_re - re) <= 1e-6 * dre, (j, g_re, re)
+        assert abs(g_dre - dre) <= 1e-6 * dre
+        assert abs(g_im - im) <= 1e-6 * max(dim, 1e-300) or (dim == 0 and g_im == 0)
+        m_re, m_dre = rmx["integral"][j][0]
+        m_im = rmx["integral"][j][1][0]
+        assert abs(m_re - re) <= 0.05 * dre, (j, m_re, re, dre)
+        assert abs(m_im - im) <= 0.05 * max(dim, 1e-300) or (dim == 0 and m_im == 0)
+
+
+SUITE_N = 10**7
+
+
+@pytest.mark.parametrize("name", sorted(PINS["suite_expectations"]))
+@pytest.mark.parametrize("precision", [ft.FP64, ft.MIXED])
+def test_reference_suite_expectations(name, precision):
+    """tests/*.txt of the reference (high-statistics epsilon expansions) within 4 sigma."""
+    p = plan(name)
+    r = p.integrate(SUITE_N, seed=0, precision=precision)
+    exp = PINS["suite_expectations"][name]
+    worst = 0.0
+    for j, ((re, dre), (im, dim)) in enumerate(exp):
+        for (g, dg), (x, dx) in ((r["integral"][j][0], (re, dre)), (r["integral"][j][1], (im, dim))):
+            sig = np.hypot(dg, dx)
+            if sig == 0:
+                assert g == x == 0
+                continue
+            worst = max(worst, abs(g - x) / sig)
+    print(name, precision, "worst deviation %.2f sigma" % worst)
+    assert worst < 4.0
+
+
+def test_json_contract_on_the_device():
+    inp = dict(PINS["cases"]["K4_masses_1to6"]["input"], N=200000)
+    out, log = ft.run_json(inp, with_log=True)
+    assert set(out) == {"IGtr", "integral", "seconds preprocessing", "seconds sampling"}
+    assert out["IGtr"] == 84.0
+    agg = PINS["cases"]["K4_masses_1to6"]["aggregate"]["integral"]
+    for j in range(3):
+        assert abs(out["integral"][j][0][0] - agg[j][0][0]) <= 1e-6 * agg[j][0][1]
+        assert out["integral"][j][1] == [0.0, 0.0]
+    assert "Euclidean" in log
