@@ -1,0 +1,349 @@
+"""Benchmark of feyntrop's tropical sampling + integrand evaluation loop on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (one step): one integration of the planar double box (6 vertices,
+7 edges, Minkowski kinematics with the contour deformation, lambda = 0.5, 2 eps
+orders) with N = 1e8 samples of the seed's xoshiro256+ stream, in mixed precision
+(FP32 integrand, FP64 sector decisions and FP64 re-evaluation of flagged samples).
+The plain-FP64 GPU form of the same step is timed beside it.  Inputs are synthetic
+(seeded kinematics); nothing is read from disk.
+
+Timing: W untimed steps, then K steps, each bracketed by CUDA events on the stream
+the kernels run on; the L2 cache is flushed (256 MiB write) between steps, outside
+the events.  A barrier and a device synchronize bracket the timed loop; the
+reported time is the max over ranks.  `e2e` repeats the step through the public
+API as a user calls it (plan creation with host preprocessing and the upload of
+the table, integration, result read-back) timed on the host.
+
+Multi-GPU (torchrun): rank r integrates its own block of N samples of the same
+stream (samples [rN, (r+1)N)); the merged moments equal a single run over all
+blocks; weak scaling.
+
+--impl reference: the reference's CPU implementation of this loop on the host
+cores (the reference binary when it is present and runs here, else the oracle's
+restatement built with the reference's compiler flags), all host threads, each
+step a bounded sample of the same workload.
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "samples/s on 1 GB300: mixed-prec batched vs plain FP64 at <=1e-5 rel err"
+UNIT = "samples/s"
+
+
+def algorithmic_flops(E, V, K, deformed):
+    """Floating-point operations per sample of the reference's algorithm (transcendentals
+    counted once each): cut scan, sector, Laplacian LDLT and solve, Minkowski: inverse,
+    L^-1 P L^-T, derivatives, complex LU and solve, Jacobian LU, complex pow/log."""
+    n = V - 1
+    f = E * (E + 1) + 8 * E + 2 * n ** 3 / 3 + 2 * n ** 3 + V * V + (E + 3) + 2
+    if deformed:
+        f += 2 * n ** 3 + 4 * n ** 3 + 5 * E * E + 8 * n ** 3 / 3 + 8 * n ** 3 + 8 * E ** 3 / 3 + E + 4
+    f += 4 * K
+    return f
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"]}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = max(float(r[2]) for r in rows if r[2].replace(".", "").isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_rate(inp, seconds, threads, kind_pref=("reference", "port")):
+    """Samples/s of the reference's CPU loop on this host: the reference binary when it
+    is built and runs here, else the restatement built with the reference's flags."""
+    ref_bin = os.path.join(HERE, "oracle", "_ref", "feyntrop")
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    if "reference" in kind_pref and os.path.exists(ref_bin):
+        try:
+            probe = subprocess.run([ref_bin], input=json.dumps(dict(inp, N=20000)), capture_output=True, text=True,
+                                   env=env, timeout=120)
+            if probe.returncode == 0:
+                r0 = 20000 / max(json.loads(probe.stdout)["seconds sampling"], 1e-6)
+                n = int(max(1e5, min(r0 * seconds, 5e8)))
+                out = subprocess.run([ref_bin], input=json.dumps(dict(inp, N=n)), capture_output=True, text=True,
+                                     env=env, timeout=600)
+                t = json.loads(out.stdout)["seconds sampling"]
+                return n / t, n, "reference"
+        except (OSError, subprocess.SubprocessError, ValueError, KeyError):
+            pass
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    import oracle_lib  # the oracle's CPU restatement: the baseline only, never the measured GPU path
+    p = oracle_lib.Prepared(inp, fast=True)
+    t0 = time.perf_counter()
+    p.integrate(50000, 0, threads)
+    r0 = 50000 / (time.perf_counter() - t0)
+    n = int(max(1e5, min(r0 * seconds, 5e8)))
+    t0 = time.perf_counter()
+    p.integrate(n, 0, threads)
+    return n / (time.perf_counter() - t0), n, "port"
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from feyntrop_gb300 import workloads
+    inp = workloads.double_box(N=args.samples)
+    threads = os.cpu_count() or 1
+    vals = []
+    kind = None
+    nsample = 0
+    for step in range(args.warmup + args.steps):
+        v, nsample, kind = cpu_rate(inp, args.ref_seconds, threads)
+        if step >= args.warmup:
+            vals.append(v)
+    value = sum(vals) / len(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": args.samples / value * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded double-box kinematics)",
+        "config": {"workload": "double box, Minkowski, lambda=0.5, 2 eps orders, N=%d per step" % args.samples,
+                   "host_threads": threads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": "%d samples of the same stream per step, rate extrapolated to N" % nsample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--samples", type=int, default=10 ** 8)
+    ap.add_argument("--ref-seconds", type=float, default=4.0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="only the timed sampling steps (for profiler captures); prints a reduced line")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import feyntrop_gb300 as ft
+    from feyntrop_gb300 import workloads
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist = None
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    N = args.samples
+    inp = workloads.double_box(N=N)
+    plan = ft.Plan(inp)
+    stream = torch.cuda.Stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed_steps(precision, K, W, tag):
+        res = []
+        times = []
+        with torch.cuda.stream(stream):
+            for s in range(W + K):
+                flush.fill_(float(s))
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                r = plan.integrate(N, seed=s, precision=precision, first_sample=rank * N,
+                                   stream=stream.cuda_stream)
+                ev1.record(stream)
+                ev1.synchronize()
+                if s >= W:
+                    times.append(ev0.elapsed_time(ev1))
+                    res.append(r)
+        return times, res
+
+    # warm-up (kernel compilation, skip matrices) outside any timing
+    timed_steps(ft.MIXED, 0, args.warmup, "warm")
+    timed_steps(ft.FP64, 0, 1, "warm")
+    barrier()
+    with ClockSampler(local) as clk:
+        barrier()
+        t_mixed, r_mixed = timed_steps(ft.MIXED, args.steps, 0, "mixed")
+        barrier()
+    clocks = clk.summary()
+    barrier()
+    fp64_steps = max(2, min(args.steps, 3))
+    t_fp64, r_fp64 = timed_steps(ft.FP64, fp64_steps, 0, "fp64")
+    barrier()
+
+    ms_mixed = sum(t_mixed) / len(t_mixed)
+    ms_fp64 = sum(t_fp64) / len(t_fp64)
+    if args.kernel_only:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": N * world / (ms_mixed * 1e-3), "unit": UNIT,
+                              "ms_per_step": ms_mixed, "fp64_ms_per_step": ms_fp64, "kernel_only": True}))
+        return
+    if dist:
+        t = torch.tensor([ms_mixed, ms_fp64], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_mixed, ms_fp64 = t.tolist()
+    value = N * world / (ms_mixed * 1e-3)
+    value64 = N * world / (ms_fp64 * 1e-3)
+
+    # per-sample error of the mixed form against the FP64 form on the same samples
+    nrec = 1 << 17
+    rm = plan.records(nrec, seed=0, precision=ft.MIXED)
+    r6 = plan.records(nrec, seed=0, precision=ft.FP64)
+    import numpy as np
+    ok = (r6["flags"] & 1) == 0
+    scale = np.abs(r6["R"][ok]).max(axis=1)
+    err = np.abs(rm["R"][ok] - r6["R"][ok]).max(axis=1) / np.where(scale > 0, scale, 1)
+    err_stats = {"samples": int(ok.sum()), "max": float(err.max()), "mean": float(err.mean()),
+                 "p99.9": float(np.quantile(err, 0.999)), "frac_above_1e-5": float((err > 1e-5).mean()),
+                 "against": "the plain-FP64 GPU form (itself checked against the CPU oracle in tests)"}
+
+    # end to end through the public API: plan (host preprocessing + upload), integrate, read back
+    barrier()
+    e2e_times = []
+    h2d = d2h = 0
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        p2 = ft.Plan(inp)
+        r = p2.integrate(N, seed=100 + s, precision=ft.MIXED, first_sample=rank * N)
+        e2e_times.append(time.perf_counter() - t0)
+        h2d = p2.info["table_bytes"] + 8 * (8 + 2 * p2.E + 64)
+        d2h = 8 * (8 * p2.K + 8) + 4
+        p2.close()
+    e2e_s = sum(e2e_times) / len(e2e_times)
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = t.item()
+
+    # merged result over ranks (moments are additive)
+    moments = r_mixed[-1]["moments"]
+    if dist:
+        allm = [None] * world
+        dist.all_gather_object(allm, moments)
+        moments = [[math.fsum(m[i][k] for m in allm) for k in range(5)] for i in range(len(moments))]
+    integral = ft.finalize_moments(moments, plan.K, real_only=not plan.info["deformed"])
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+
+    fp32_peak, fp64_peak = ft.device_peaks()
+    flops = algorithmic_flops(plan.E, plan.V, plan.K, bool(plan.info["deformed"]))
+    launches = sum(r["kernel_launches"] for r in r_mixed)
+    fallback = sum(r["fp64_fallback"] for r in r_mixed) / (N * len(r_mixed))
+    acc0 = integral[0][0][1]
+    sigma1 = acc0 * math.sqrt(N * world)
+    target = 1e-4 * abs(integral[0][0][0])
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        threads = os.cpu_count() or 1
+        v, nsample, kind = cpu_rate(inp, args.cpu_seconds, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": "%d samples of the double-box workload (same stream), all host threads" % nsample}
+    prof = os.path.join(HERE, "profiles", "traffic.json")
+    traffic = None
+    if os.path.exists(prof):
+        traffic = json.load(open(prof)).get("ft_sample_mixed_double_box_bytes_per_launch")
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 integrand, f64 sector decisions and fallback",
+        "data": "synthetic (seeded double-box kinematics, Random(1))",
+        "config": {"workload": "double box (6 vertices, 7 edges), Minkowski, lambda=0.5, D=4, 2 eps orders, "
+                               "N=%d samples per step per GPU" % N,
+                   "precision": "mixed", "parallelism": "sample blocks of one stream per GPU",
+                   "l2": "flushed between steps (256 MiB write), per-step CUDA events on the kernels' stream"},
+        "plain_fp64": {"value": value64, "ms_per_step": ms_fp64, "steps": len(t_fp64),
+                       "roofline": {"bound": "fp64", "achieved": flops * value64 / world / 1e12,
+                                    "peak": fp64_peak, "unit": "TFLOP/s",
+                                    "frac": flops * value64 / world / 1e12 / fp64_peak}},
+        "mixed_over_fp64": value / value64,
+        "per_sample_error": err_stats,
+        "fp64_fallback_rate": fallback,
+        "integral": integral,
+        "time_to_target_sigma_s": {"target": "1e-4 * |Re I0|", "mixed": (sigma1 / target) ** 2 / value,
+                                   "fp64": (sigma1 / target) ** 2 / value64},
+        "roofline": {"bound": "fp32", "achieved": flops * value / world / 1e12, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": flops * value / world / 1e12 / fp32_peak, "traffic": traffic,
+                     "note": "algorithmic flops per sample %.0f (reference algorithm); peak = FP32 FMA issue "
+                             "rate measured live by an FMA-chain probe (FP64: %.2f TFLOP/s)" % (flops, fp64_peak)},
+        "e2e": {"value": N * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -34,7 +34,7 @@ MIXED = 1
 
 EXPORTED = ["ft_plan_create", "ft_plan_destroy", "ft_plan_get_info", "ft_plan_log_line", "ft_integrate",
             "ft_integrate_batch", "ft_finalize_moments", "ft_sample_records", "ft_run_json", "ft_free",
-            "ft_precompile", "ft_last_error", "ft_version"]
+            "ft_precompile", "ft_last_error", "ft_version", "ft_subgraph_table", "ft_device_peaks"]
 
 
 class FeyntropError(RuntimeError):
@@ -105,6 +105,7 @@ def lib():
                                       ctypes.POINTER(ctypes.c_void_p)]
             L.ft_free.argtypes = [ctypes.c_void_p]
             L.ft_precompile.argtypes = [ctypes.POINTER(Problem), ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+            L.ft_device_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             L.ft_subgraph_table.argtypes = [ctypes.POINTER(Problem)] + [ctypes.c_void_p] * 4 + [
                 ctypes.POINTER(PlanInfo)]
             _lib = L
@@ -148,6 +149,13 @@ def subgraph_table(inp):
     info = PlanInfo()
     _check(lib().ft_subgraph_table(ctypes.byref(a.struct), _ptr(Jr), _ptr(r), _ptr(mm), _ptr(L), ctypes.byref(info)))
     return Jr, r, mm, L, {f: getattr(info, f) for f, _ in PlanInfo._fields_}
+
+
+def device_peaks():
+    """Measured (FP32, FP64) FMA issue rates of the current device in TFLOP/s."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _check(lib().ft_device_peaks(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def precompile(inp, precision=MIXED):

@@ -99,9 +99,59 @@ __global__ void ft_finalize_parts(const double* __restrict__ parts, int nparts, 
     }
 }
 
+// Issue-rate probes for the roofline denominators: every thread runs 8 independent
+// FMA chains, so the pipe, not the dependency latency, limits the rate.
+template <class T>
+__global__ void __launch_bounds__(256) ft_fma_probe(T* __restrict__ out, int iters, T a, T b)
+{
+    T x[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = (T)(threadIdx.x + k) * (T)1e-3;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int k = 0; k < 8; k++) x[k] = x[k] * a + b;
+    }
+    T s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; k++) s += x[k];
+    if (s == (T)12345.678) out[threadIdx.x] = s;   // keeps the chains alive
+}
+
 }  // namespace
 
 namespace ft {
+
+// FMA issue rate in TFLOP/s (2 flops per FMA), timed with CUDA events
+double fma_peak_tflops(bool fp64)
+{
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    void* buf = nullptr;
+    cudaMalloc(&buf, 4096);
+    const int blocks = sms * 8, iters = fp64 ? 2048 : 65536;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    float best = 1e30f;
+    for (int rep = 0; rep < 4; rep++) {
+        cudaEventRecord(e0);
+        if (fp64)
+            ft_fma_probe<double><<<blocks, 256>>>((double*)buf, iters, 0.999999, 1e-7);
+        else
+            ft_fma_probe<float><<<blocks, 256>>>((float*)buf, iters, 0.999999f, 1e-7f);
+        cudaEventRecord(e1);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(buf);
+    const double flops = 2.0 * 8 * (double)iters * blocks * 256;
+    return flops / (best * 1e-3) / 1e12;
+}
 
 cudaError_t launch_lane_powers(const u64* tpow, u64 S, int nbits, u64* out, cudaStream_t st)
 {

@@ -12,4 +12,7 @@ cudaError_t launch_lane_powers(const unsigned long long* tpow, unsigned long lon
 // out[s] = sum over parts of parts[p * slots + s]; slots [0, ndd) are (hi, lo) pairs
 cudaError_t launch_finalize(const double* parts, int nparts, int slots, int ndd, double* out, cudaStream_t st);
 
+// FMA issue-rate probe (TFLOP/s, FMA = 2 flops) of the current device
+double fma_peak_tflops(bool fp64);
+
 }  // namespace ft

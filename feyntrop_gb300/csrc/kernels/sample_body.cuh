@@ -47,6 +47,11 @@
 typedef unsigned long long u64;
 typedef unsigned int u32;
 
+// intermediate values for host-side numerical studies (compiled out on the device)
+#ifndef FT_DBG
+#define FT_DBG(slot, value)
+#endif
+
 #define FT_N (FT_V - 1)
 #define FT_FULL ((1u << FT_E) - 1u)
 #define FT_NPAIR (FT_E * (FT_E - 1) / 2)
@@ -961,6 +966,7 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
     float xnu = 0.0f, thsum = 0.0f;
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
+        FT_DBG(e, theta[e]);
         float sn, cs;
         sincosf(theta[e], &sn, &cs);
         cX[e] = cmk(X[e] * cs, X[e] * sn);
@@ -1004,6 +1010,10 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
         mag += pf[P_M2 + e] * X[e];
     }
     const float vabs = cabs_(cV);
+    FT_DBG(20, cV.re);
+    FT_DBG(21, cV.im);
+    FT_DBG(22, cpphi.re);
+    FT_DBG(23, cpphi.im);
     if (!(vabs > 1e-3f * mag)) {
         need64 = true;
         return false;
@@ -1038,6 +1048,10 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
             for (int j = i; j < FT_E; j++) J[i][j] = J[i][j] - f * J[k][j];
         }
     }
+    FT_DBG(24, (float)mj.e + log2f(mj.m));
+    FT_DBG(25, atan2f(pj.im, pj.re));
+    FT_DBG(26, apsi);
+    FT_DBG(27, growth);
     if (edge || cpsi.bad || mv.bad || mj.bad) {
         need64 = true;
         return false;
@@ -1073,6 +1087,7 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
 }
 #endif
 
+#ifndef FT_HOST_SIM
 // ------------------------------------------------------------------ accumulation
 // Neumaier-compensated running sums per thread
 struct nsum {
@@ -1470,3 +1485,4 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue(
     A.finish(acc_out);
 }
 #endif
+#endif  // FT_HOST_SIM

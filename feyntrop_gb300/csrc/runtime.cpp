@@ -568,6 +568,22 @@ int ft_precompile(const ft_problem* pb, int32_t precision, double* seconds)
     }
 }
 
+int ft_device_peaks(double* fp32, double* fp64)
+{
+    try {
+        require_device();
+        if (fp32) *fp32 = ft::fma_peak_tflops(false);
+        if (fp64) *fp64 = ft::fma_peak_tflops(true);
+        cu(cudaGetLastError(), "probe kernels");
+        return FT_OK;
+    } catch (const std::logic_error& e) {
+        g_error = e.what();
+        return FT_ERR_NO_DEVICE;
+    } catch (...) {
+        return status_of(std::current_exception());
+    }
+}
+
 int ft_finalize_moments(const ft_moments* m, int32_t K, int32_t real_only, ft_result* r)
 {
     // srcs/stats.hpp:86-104 on the merged sums (long double for the final arithmetic)

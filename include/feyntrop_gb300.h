@@ -140,6 +140,10 @@ int ft_subgraph_table(const ft_problem* problem, double* Jr, double* r, uint8_t*
  * warms the kernel cache.  *seconds receives the compile time (0 when cached). */
 int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds);
 
+/* Measured FP32 and FP64 FMA issue rates of the current device in TFLOP/s (an
+ * FMA-chain probe kernel; the denominators of the sampling kernels' roofline). */
+int ft_device_peaks(double* fp32_tflops, double* fp64_tflops);
+
 const char* ft_last_error(void);
 const char* ft_version(void);
 

@@ -72,22 +72,32 @@ static bitmat mul(const bitmat& A, const bitmat& B)
     return C;
 }
 
+// T^(2^b), b = 0..63, built once
+static const std::vector<bitmat>& powers()
+{
+    static const std::vector<bitmat> P = [] {
+        std::vector<bitmat> v(64);
+        bitmat T(256);
+        for (int c = 0; c < 256; c++) {
+            xoshiro x(0);
+            for (int w = 0; w < 4; w++) x.s[w] = 0;
+            x.s[c >> 6] = 1ULL << (c & 63);
+            x.next();
+            for (int w = 0; w < 4; w++) T[c][w] = x.s[w];
+        }
+        v[0] = T;
+        for (int b = 1; b < 64; b++) v[b] = mul(v[b - 1], v[b - 1]);
+        return v;
+    }();
+    return P;
+}
+
 void skip(xoshiro& g, uint64_t steps)
 {
-    bitmat T(256);
-    for (int c = 0; c < 256; c++) {
-        xoshiro x(0);
-        for (int w = 0; w < 4; w++) x.s[w] = 0;
-        x.s[c >> 6] = 1ULL << (c & 63);
-        x.next();
-        for (int w = 0; w < 4; w++) T[c][w] = x.s[w];
-    }
+    const std::vector<bitmat>& P = powers();
     bitvec v{g.s[0], g.s[1], g.s[2], g.s[3]};
-    while (steps) {
-        if (steps & 1) v = mat_apply(T, v);
-        steps >>= 1;
-        if (steps) T = mul(T, T);
-    }
+    for (int b = 0; b < 64; b++)
+        if ((steps >> b) & 1) v = mat_apply(P[b], v);
     for (int w = 0; w < 4; w++) g.s[w] = v[w];
 }
 
@@ -175,12 +185,17 @@ struct ldlt {
     int n = 0;
     std::vector<int> perm;        // position -> original index
     std::vector<double> L, D;     // unit lower factor (row major), diagonal
+    std::vector<double> diag, y, col;
 
-    explicit ldlt(const std::vector<double>& A, int n_) : n(n_)
+    ldlt() = default;
+    ldlt(const std::vector<double>& A, int n_) { compute(A, n_); }
+
+    void compute(const std::vector<double>& A, int n_)
     {
+        n = n_;
         perm.resize(n);
+        diag.resize(n);
         for (int i = 0; i < n; i++) perm[i] = i;
-        std::vector<double> diag(n);
         for (int i = 0; i < n; i++) diag[i] = A[i * n + i];
         for (int k = 0; k < n; k++) {
             int best = k;
@@ -208,10 +223,10 @@ struct ldlt {
         }
     }
 
-    // A^{-1} b for one column
-    std::vector<double> solve(const std::vector<double>& b) const
+    // x = A^{-1} b (x and b may not alias)
+    void solve_into(const double* b, double* x)
     {
-        std::vector<double> y(n);
+        y.resize(n);
         for (int i = 0; i < n; i++) y[i] = b[perm[i]];
         for (int i = 0; i < n; i++)
             for (int j = 0; j < i; j++) y[i] -= L[i * n + j] * y[j];
@@ -219,8 +234,13 @@ struct ldlt {
             y[i] = std::fabs(D[i]) > std::numeric_limits<double>::min() ? y[i] / D[i] : 0.0;
         for (int i = n - 1; i >= 0; i--)
             for (int j = i + 1; j < n; j++) y[i] -= L[j * n + i] * y[j];
-        std::vector<double> x(n);
         for (int i = 0; i < n; i++) x[perm[i]] = y[i];
+    }
+
+    std::vector<double> solve(const std::vector<double>& b)
+    {
+        std::vector<double> x(n);
+        solve_into(b.data(), x.data());
         return x;
     }
 
@@ -232,13 +252,14 @@ struct ldlt {
     }
 
     // trace(A^{-1} B), B row major n x n
-    double trace_solve(const std::vector<double>& B) const
+    double trace_solve(const std::vector<double>& B)
     {
         double t = 0.0;
-        std::vector<double> col(n);
+        col.resize(2 * n);
         for (int j = 0; j < n; j++) {
             for (int i = 0; i < n; i++) col[i] = B[i * n + j];
-            t += solve(col)[j];
+            solve_into(col.data(), col.data() + n);
+            t += col[n + j];
         }
         return t;
     }
@@ -247,13 +268,21 @@ struct ldlt {
 // LU with complete pivoting (largest modulus, first in column-major order), as used
 // at srcs/feynman_integral.hpp:305.
 struct full_piv_lu {
-    int n;
+    int n = 0;
     std::vector<cd> lu;
     std::vector<int> rowp, colp;   // transpositions
     int ntransp = 0;
 
-    full_piv_lu(std::vector<cd> A, int n_) : n(n_), lu(std::move(A)), rowp(n_), colp(n_)
+    full_piv_lu() = default;
+    full_piv_lu(std::vector<cd> A, int n_) { compute(A, n_); }
+
+    void compute(const std::vector<cd>& A, int n_)
     {
+        n = n_;
+        lu = A;
+        rowp.assign(n, 0);
+        colp.assign(n, 0);
+        ntransp = 0;
         for (int k = 0; k < n; k++) {
             int br = k, bc = k;
             double best = -1.0;
@@ -305,7 +334,7 @@ struct full_piv_lu {
 
 // LU with partial pivoting (largest modulus in the column, first wins), as used at
 // srcs/feynman_integral.hpp:314-316; only the determinant is needed.
-static cd partial_piv_det(std::vector<cd> lu, int n)
+static cd partial_piv_det(std::vector<cd>& lu, int n)
 {
     int ntransp = 0;
     for (int k = 0; k < n; k++) {
@@ -372,7 +401,8 @@ static bool mass_momentum_spanning(const problem& p, uint64_t sub, const std::ve
     double sum = 0;
     for (size_t i = 0; i < Xs.size(); i++) {
         auto La = reduced_laplacian<double>(p, sub, C, cmap, Xinvs[i]);
-        ldlt f(La, C - 1);
+        static thread_local ldlt f;
+        f.compute(La, C - 1);
         double pxi = -f.trace_solve(PGP);
         for (int j = 0; j < p.E; j++)
             if (!((sub >> j) & 1)) pxi += p.m2[j] * Xs[i][j];
@@ -742,7 +772,8 @@ sample_value evaluate(const prepared& pr, const sector& sec)
     for (int j = 0; j < E; j++) Xinv[j] = 1.0 / X[j];
 
     auto La = reduced_laplacian<double>(p, 0, V, cmap, Xinv);
-    ldlt f(La, n);
+    static thread_local ldlt f;
+    f.compute(La, n);
     double Xprod = 1.0;
     for (double x : X) Xprod *= x;
 
@@ -779,16 +810,20 @@ sample_value evaluate(const prepared& pr, const sector& sec)
 
     // deformed (Minkowski) branch
     auto PGP = pgp_matrix(p, V, cmap);
-    std::vector<double> Ginv((size_t)n * n);
+    static thread_local std::vector<double> Ginv;
+    Ginv.assign((size_t)n * n, 0.0);
     {
-        std::vector<double> col(n);
+        static thread_local std::vector<double> col;
+        col.assign(2 * n, 0.0);
         for (int j = 0; j < n; j++) {
             for (int i = 0; i < n; i++) col[i] = (i == j) ? 1.0 : 0.0;
-            auto x = f.solve(col);
-            for (int i = 0; i < n; i++) Ginv[i * n + j] = x[i];
+            f.solve_into(col.data(), col.data() + n);
+            for (int i = 0; i < n; i++) Ginv[i * n + j] = col[n + i];
         }
     }
-    std::vector<double> T1((size_t)n * n, 0.0), M((size_t)n * n, 0.0);
+    static thread_local std::vector<double> T1, M;
+    T1.assign((size_t)n * n, 0.0);
+    M.assign((size_t)n * n, 0.0);
     for (int i = 0; i < n; i++)
         for (int j = 0; j < n; j++) {
             double s = 0;
@@ -801,13 +836,18 @@ sample_value evaluate(const prepared& pr, const sector& sec)
             for (int k = 0; k < n; k++) s += T1[i * n + k] * Ginv[j * n + k];
             M[i * n + j] = s;
         }
-    std::vector<double> Xinv2(E);
+    static thread_local std::vector<double> Xinv2;
+    Xinv2.assign(E, 0.0);
     for (int j = 0; j < E; j++) Xinv2[j] = Xinv[j] * Xinv[j];
-    std::vector<double> d(E), dd((size_t)E * E);
+    static thread_local std::vector<double> d, dd;
+    d.assign(E, 0.0);
+    dd.assign((size_t)E * E, 0.0);
     pphi_derivatives(p, V, cmap, Xinv, Xinv2, Ginv, M, d, dd);
     for (int j = 0; j < E; j++) d[j] = (d[j] + p.m2[j]) * pr.def_ref;
 
-    std::vector<cd> cX(E), cXinv(E);
+    static thread_local std::vector<cd> cX, cXinv;
+    cX.assign(E, cd(0, 0));
+    cXinv.assign(E, cd(0, 0));
     for (int j = 0; j < E; j++) {
         cX[j] = X[j] * cd(std::cos(d[j]), std::sin(d[j]));
         cXinv[j] = 1.0 / cX[j];
@@ -815,13 +855,15 @@ sample_value evaluate(const prepared& pr, const sector& sec)
     auto cLa = reduced_laplacian<cd>(p, 0, V, cmap, cXinv);
     for (int k = 0; k < n; k++)
         for (int l = k + 1; l < n; l++) cLa[k * n + l] = cLa[l * n + k];
-    full_piv_lu lu(cLa, n);
+    static thread_local full_piv_lu lu;
+    lu.compute(cLa, n);
     cd cXprod = 1.0;
     for (auto& c : cX) cXprod *= c;
     cd cPsi = cXprod * lu.det();
     cd cR = pr.IGtr * cpow(cPsi, -D / 2.);
 
-    std::vector<cd> J((size_t)E * E);
+    static thread_local std::vector<cd> J;
+    J.assign((size_t)E * E, cd(0, 0));
     for (int a = 0; a < E; a++)
         for (int b = 0; b < E; b++)
             J[a * E + b] = cd(0., pr.def_ref) * dd[a * E + b] * X[b] + (a == b ? 1.0 : 0.0);
@@ -927,10 +969,18 @@ estimate integrate(const prepared& pr, uint64_t N, uint64_t seed, int threads)
     std::vector<std::vector<stats>> re(threads, std::vector<stats>(K)), im(threads, std::vector<stats>(K));
     std::vector<uint64_t> dropped(threads, 0);
     const bool real_only = !pr.deformed();
-#pragma omp parallel for num_threads(threads) schedule(static, 1)
-    for (int t = 0; t < threads; t++) {
-        uint64_t lo = N / threads * t + std::min<uint64_t>(t, N % threads);
-        uint64_t hi = lo + N / threads + (t < (int)(N % threads) ? 1 : 0);
+    powers();
+    // chunks of the single stream; a chunk's first state is reached by skip-ahead,
+    // so every sample is the one the single-threaded reference would draw
+    const uint64_t chunk = 10000, nchunks = (N + chunk - 1) / chunk;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 1)
+    for (uint64_t c = 0; c < nchunks; c++) {
+#ifdef _OPENMP
+        const int t = omp_get_thread_num();
+#else
+        const int t = 0;
+#endif
+        const uint64_t lo = c * chunk, hi = std::min(N, lo + chunk);
         xoshiro g(seed);
         skip(g, lo * (uint64_t)(2 * E - 1));
         for (uint64_t i = lo; i < hi; i++) {
@@ -953,12 +1003,13 @@ estimate integrate(const prepared& pr, uint64_t N, uint64_t seed, int threads)
                 }
             }
         }
-        if (real_only)
+    }
+    if (real_only)
+        for (int t = 0; t < threads; t++)
             for (int j = 0; j < K; j++) {
                 im[t][j].update(0);
                 im[t][j].update(0);
             }
-    }
     estimate est;
     for (int j = 0; j < K; j++) {
         std::vector<stats> rj, ij;

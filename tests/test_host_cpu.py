@@ -29,7 +29,7 @@ def test_every_declared_function_is_exported():
     L = ft.lib()
     for n in names:
         assert hasattr(L, n), n
-    assert set(names) <= set(ft.EXPORTED) | {"ft_subgraph_table"}
+    assert set(names) <= set(ft.EXPORTED)
 
 
 @pytest.mark.parametrize("name", sorted(PINS["cases"]))
