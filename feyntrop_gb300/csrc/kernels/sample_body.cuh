@@ -425,23 +425,30 @@ static __device__ __forceinline__ f2 f2_add2(f2 a, f2 b)
     return f2_add(r, b.lo);
 }
 
-// log(1 - u) for u = (x >> 11) 2^-53, to a few 1e-8 absolute
+// log(1 - u) for u = (x >> 11) 2^-53, to about 1e-7 absolute, with integer and FP32
+// instructions only (64-bit integer to float conversions would run on the FP64 pipe).
+// A positive integer v is turned into the float bits of 2^k (1 + f) directly: k from
+// the leading-zero count, f from the next 23 bits rounded (a carry bumps k).
+static __device__ __forceinline__ int float_bits_of(u64 v, int scale_exp)
+{
+    const int lz = __clzll(v);
+    const u64 frac = ((((v << lz) << 1) >> 40) + 1ull) >> 1;   // 23 bits after the leading 1, rounded
+    return ((63 - lz + scale_exp + 127) << 23) + (int)frac;
+}
+
 static __device__ __forceinline__ f2 log1m_u(u64 x)
 {
     const u64 m = x >> 11;
     f2 r;
+    r.lo = 0.0f;
     if (m < (1ull << 52)) {
-        // u < 1/2: log1p(-u), u rounded to float (relative 2^-24 -> absolute < 2^-24)
-        r.hi = log1pf(-__ull2float_rn(m) * 0x1.0p-53f);
-        r.lo = 0.0f;
+        // u < 1/2: log1p(-u)
+        r.hi = m ? log1pf(-__int_as_float(float_bits_of(m, -53))) : 0.0f;
         return r;
     }
-    // 1 - u = q 2^-53 with q < 2^52 exact; q rounded to float = 2^k (1 + f),
-    // log(1 - u) = (k - 53) ln2 + log1p(f) with f exact
-    const u64 q = (1ull << 53) - m;
-    const float qf = __ull2float_rn(q);
-    const int bits = __float_as_int(qf);
-    const int k = ((bits >> 23) & 0xff) - 127;
+    // 1 - u = q 2^-53 exactly (q < 2^52); q = 2^k (1 + f): log(1 - u) = (k - 53) ln2 + log1p(f)
+    const int bits = float_bits_of((1ull << 53) - m, 0);
+    const int k = (bits >> 23) - 127;
     const float f = __int_as_float((bits & 0x007fffff) | 0x3f800000) - 1.0f;
     const float kk = (float)(k - 53);
     // ln2 split so that kk * LN2_HI is exact
@@ -740,6 +747,89 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
 
 // ------------------------------------------------------------------ integrand, mixed
 #if FT_PREC == 1
+#if FT_MODE == 1
+// x-derivatives of phi/psi at the sample point (srcs/laplacian.hpp:102-215) and the
+// deformation angle theta = -lambda (d(phi/psi)/dx + m^2) (srcs/feynman_integral.hpp:290-291),
+// in FP64 from FP32 conductances; outputs theta and the upper triangle of H.
+static __device__ __forceinline__ void derivatives64(const float* Xi32, const double* prm, float* theta_out,
+                                                     float (*H_out)[FT_E])
+{
+    double Xi[FT_E];
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) Xi[e] = (double)Xi32[e];
+    elim<double, double> L;
+    L.factor(Xi);
+    double Nm[FT_N][FT_N];
+#pragma unroll
+    for (int i = FT_N - 1; i >= 0; i--) {
+#pragma unroll
+        for (int j = 0; j < FT_N; j++) Nm[i][j] = 0.0;
+        Nm[i][i] = 1.0;
+#pragma unroll
+        for (int j = i + 1; j < FT_N; j++) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = i + 1; k <= j; k++) s = fma(L.a[i][k], Nm[k][j], s);
+            Nm[i][j] = s;
+        }
+    }
+    double id[FT_N];
+#pragma unroll
+    for (int k = 0; k < FT_N; k++) id[k] = 1.0 / L.d[k];
+    double G[FT_N][FT_N];
+#pragma unroll
+    for (int i = 0; i < FT_N; i++)
+#pragma unroll
+        for (int j = i; j < FT_N; j++) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = j; k < FT_N; k++) s = fma(Nm[i][k] * Nm[j][k], id[k], s);
+            G[i][j] = s;
+            G[j][i] = s;
+        }
+    double hb[FT_RANK][FT_E];
+#pragma unroll
+    for (int r = 0; r < FT_RANK; r++) {
+        double h[FT_N];
+#pragma unroll
+        for (int i = 0; i < FT_N; i++) {
+            double s = 0.0;
+#pragma unroll
+            for (int j = 0; j < FT_N; j++) s = fma(G[i][j], prm[P_Q + r * FT_N + j], s);
+            h[i] = s;
+        }
+#pragma unroll
+        for (int e = 0; e < FT_E; e++) {
+            const int k = FT_EK[e], l = FT_EL[e];
+            hb[r][e] = (k == FT_V - 1 ? 0.0 : h[k]) - h[l];
+        }
+    }
+    auto Gx = [&](int i, int j) -> double { return (i == FT_V - 1 || j == FT_V - 1) ? 0.0 : G[i][j]; };
+    const double kappa = prm[P_DEF];
+#pragma unroll
+    for (int a = 0; a < FT_E; a++) {
+        const int ka = FT_EK[a], la = FT_EL[a];
+        double s = 0.0;
+#pragma unroll
+        for (int r = 0; r < FT_RANK; r++) s = fma(prm[P_SIG + r] * hb[r][a], hb[r][a], s);
+        const double t = Gx(ka, ka) + Gx(la, la) - 2.0 * Gx(ka, la);
+        const double xa = Xi[a] * Xi[a];
+        const double xas = xa * s;
+        theta_out[a] = (float)((prm[P_M2 + a] - xas) * kappa);
+        H_out[a][a] = (float)(2.0 * xas * (Xi[a] - xa * t));
+#pragma unroll
+        for (int b = a + 1; b < FT_E; b++) {
+            const int kb = FT_EK[b], lb = FT_EL[b];
+            double s2 = 0.0;
+#pragma unroll
+            for (int r = 0; r < FT_RANK; r++) s2 = fma(prm[P_SIG + r] * hb[r][a], hb[r][b], s2);
+            const double t2 = Gx(ka, kb) + Gx(la, lb) - Gx(ka, lb) - Gx(la, kb);
+            H_out[a][b] = (float)(-2.0 * xa * (Xi[b] * Xi[b]) * s2 * t2);
+        }
+    }
+}
+#endif
+
 // positive value m * 2^e with m in [1, 2): products of many pivots and X values
 // without overflow, and logarithms split into an exact integer and a small part
 struct mexp {
@@ -786,6 +876,14 @@ static __device__ __forceinline__ f2 f2_mul2(f2 a, f2 b)
     return f2_make(h, e - (h - p));
 }
 static __device__ __forceinline__ f2 f2_neg(f2 a) { return f2_make(-a.hi, -a.lo); }
+// relative size of V below which the FP32 evaluation hands the sample to FP64
+#ifndef V_CANCEL
+#define V_CANCEL 0.05f
+#endif
+// smallest pivot-to-row ratio accepted in the FP32 complex eliminations
+#ifndef PIVOT_GROWTH
+#define PIVOT_GROWTH 0.03f
+#endif
 #define RLN2_HI 1.44269502162933349609375f
 #define RLN2_LO 1.925963033500011e-8f
 #define LN2_F 0.69314718055994531f
@@ -810,8 +908,8 @@ static __device__ __forceinline__ float wrap_pi(float x, bool& edge)
     return r;
 }
 
-static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx, f2 lF, f2 lG, cx<float>* out,
-                                                   bool& need64)
+static __device__ __forceinline__ bool integrand32(const double* prm, const float* pf, const f2* lx, f2 lF, f2 lG,
+                                                   cx<float>* out, bool& need64)
 {
     need64 = false;
     const float D2 = 0.5f * pf[P_D], W = pf[P_W];
@@ -865,7 +963,7 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
         pxi += v;
         mag += fabsf(v);
     }
-    if (!(pxi > 1e-3f * mag)) {   // cancellation, or a sign the FP64 pass must judge
+    if (!(pxi > V_CANCEL * mag)) {   // cancellation, or a sign the FP64 pass must judge
         need64 = true;
         return false;
     }
@@ -892,76 +990,11 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
 #endif
 #else
     const float kappa = pf[P_DEF];
-    // G = L^-1 = N diag(1/d) N^T, N = M^-1 (entrywise non-negative)
-    float Nm[FT_N][FT_N];
-#pragma unroll
-    for (int i = FT_N - 1; i >= 0; i--) {
-#pragma unroll
-        for (int j = 0; j < FT_N; j++) Nm[i][j] = 0.0f;
-        Nm[i][i] = 1.0f;
-#pragma unroll
-        for (int j = i + 1; j < FT_N; j++) {
-            float s = 0.0f;
-#pragma unroll
-            for (int k = i + 1; k <= j; k++) s = fmaf(L.a[i][k], Nm[k][j], s);
-            Nm[i][j] = s;
-        }
-    }
-    float id[FT_N];
-#pragma unroll
-    for (int k = 0; k < FT_N; k++) id[k] = 1.0f / L.d[k];
-    float G[FT_N][FT_N];
-#pragma unroll
-    for (int i = 0; i < FT_N; i++)
-#pragma unroll
-        for (int j = i; j < FT_N; j++) {
-            float s = 0.0f;
-#pragma unroll
-            for (int k = j; k < FT_N; k++) s = fmaf(Nm[i][k] * Nm[j][k], id[k], s);
-            G[i][j] = s;
-            G[j][i] = s;
-        }
-    float hb[FT_RANK][FT_E];
-#pragma unroll
-    for (int r = 0; r < FT_RANK; r++) {
-        float h[FT_N];
-#pragma unroll
-        for (int i = 0; i < FT_N; i++) {
-            float s = 0.0f;
-#pragma unroll
-            for (int j = 0; j < FT_N; j++) s = fmaf(G[i][j], pf[P_Q + r * FT_N + j], s);
-            h[i] = s;
-        }
-#pragma unroll
-        for (int e = 0; e < FT_E; e++) {
-            const int k = FT_EK[e], l = FT_EL[e];
-            hb[r][e] = (k == FT_V - 1 ? 0.0f : h[k]) - h[l];
-        }
-    }
-    auto Gx = [&](int i, int j) -> float { return (i == FT_V - 1 || j == FT_V - 1) ? 0.0f : G[i][j]; };
+    // The contour (theta) and its Jacobian come from differences of entries of L^-1,
+    // which cancel in FP32 for a sizeable fraction of sectors; this block runs in FP64.
     float theta[FT_E];
     float H[FT_E][FT_E];
-#pragma unroll
-    for (int a = 0; a < FT_E; a++) {
-        const int ka = FT_EK[a], la = FT_EL[a];
-        float s = 0.0f;
-#pragma unroll
-        for (int r = 0; r < FT_RANK; r++) s = fmaf(pf[P_SIG + r] * hb[r][a], hb[r][a], s);
-        const float t = Gx(ka, ka) + Gx(la, la) - 2.0f * Gx(ka, la);
-        const float xa = Xi[a] * Xi[a];
-        const float xas = xa * s;
-        theta[a] = (-xas + pf[P_M2 + a]) * kappa;
-        H[a][a] = 2.0f * xas * (Xi[a] - xa * t);
-#pragma unroll
-        for (int b = a + 1; b < FT_E; b++) {
-            const int kb = FT_EK[b], lb = FT_EL[b];
-            float s2 = 0.0f;
-#pragma unroll
-            for (int r = 0; r < FT_RANK; r++) s2 = fmaf(pf[P_SIG + r] * hb[r][a], hb[r][b], s2);
-            const float t2 = Gx(ka, kb) + Gx(la, lb) - Gx(ka, lb) - Gx(la, kb);
-            H[a][b] = -2.0f * xa * (Xi[b] * Xi[b]) * s2 * t2;
-        }
-    }
+    derivatives64(Xi, prm, theta, H);
     cx<float> cX[FT_E], cy[FT_E];
     float xnu = 0.0f, thsum = 0.0f;
 #pragma unroll
@@ -976,7 +1009,8 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
     }
     elim<cx<float>, float> CL;
     const float growth = CL.factor(cy);
-    if (!(growth > 1e-3f)) {
+    // a pivot much smaller than the conductances summed into it loses ~1e-7 / growth
+    if (!(growth > PIVOT_GROWTH)) {
         need64 = true;
         return false;
     }
@@ -1014,7 +1048,9 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
     FT_DBG(21, cV.im);
     FT_DBG(22, cpphi.re);
     FT_DBG(23, cpphi.im);
-    if (!(vabs > 1e-3f * mag)) {
+    // V cancels near thresholds: its FP32 error is ~ 1e-7 * mag / |V|, so samples where
+    // |V| < V_CANCEL * mag go to the FP64 pass
+    if (!(vabs > V_CANCEL * mag)) {
         need64 = true;
         return false;
     }
@@ -1033,10 +1069,15 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
         for (int b = a; b < FT_E; b++) J[a][b] = cmk(a == b ? 1.0f : 0.0f, kappa * H[a][b] * sx[a] * sx[b]);
     mexp mj = mx_one();
     cx<float> pj = cmk(1.0f, 0.0f);
+    float jgrowth = 1.0f;
 #pragma unroll
     for (int k = 0; k < FT_E; k++) {
         const cx<float> piv = J[k][k];
         const float m = cabs_(piv);
+        float row = m;
+#pragma unroll
+        for (int j = k + 1; j < FT_E; j++) row += fabsf(J[k][j].re) + fabsf(J[k][j].im);
+        jgrowth = fminf(jgrowth, m / row);
         mx_mul(mj, m);
         const float im = 1.0f / m;
         pj = pj * cmk(piv.re * im, piv.im * im);
@@ -1052,7 +1093,7 @@ static __device__ __forceinline__ bool integrand32(const float* pf, const f2* lx
     FT_DBG(25, atan2f(pj.im, pj.re));
     FT_DBG(26, apsi);
     FT_DBG(27, growth);
-    if (edge || cpsi.bad || mv.bad || mj.bad) {
+    if (edge || cpsi.bad || mv.bad || mj.bad || !(jgrowth > PIVOT_GROWTH)) {
         need64 = true;
         return false;
     }
@@ -1430,7 +1471,7 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample(
         if (FT_RECORD)
             for (int e = 0; e < FT_E; e++) rec_X[i * FT_E + e] = exp((double)lx[e].hi + (double)lx[e].lo);
         bool need64 = false;
-        const bool ok = integrand32(pf, lx, lF, lG, R, need64);
+        const bool ok = integrand32(prm, pf, lx, lF, lG, R, need64);
         if (need64) {
             flags |= REC_QUEUED;
             A.note32(0.0f, 1.0f, (float)ex);

@@ -24,9 +24,13 @@ N_REC = 4096
 
 # per-sample relative error, |R_gpu - R_oracle| / max_j |R_oracle_j| of the sample
 FP64_MEDIAN_TOL = 1e-12
-FP64_MAX_TOL = 1e-7      # ill-conditioned sectors: both are FP64 solutions of the same system
+# In ill-conditioned sectors the reference's own FP64 algorithm (pivoted LDLT of the
+# Laplacian, derivatives from its inverse) loses up to ~2e-7; the GPU's conductance-form
+# elimination stays within ~1e-10 of a 50-digit evaluation there
+# (test_fp64_disagreements_refereed_at_high_precision).
+FP64_MAX_TOL = 1e-6
 MIXED_P999_TOL = 1e-5    # 99.9 % of the samples
-MIXED_MAX_TOL = 1e-3
+MIXED_MAX_TOL = 3e-5
 
 _plans = {}
 
@@ -71,6 +75,25 @@ def test_mixed_samples_match_oracle(name):
         np.median(err), np.quantile(err, 0.999), err.max(), queued))
     assert np.quantile(err, 0.999) < MIXED_P999_TOL
     assert err.max() < MIXED_MAX_TOL
+
+
+@pytest.mark.parametrize("name", ["C2_double_box", "2L_4pt_ladder", "C3_box_pentagon_1"])
+def test_fp64_disagreements_refereed_at_high_precision(name):
+    mp = pytest.importorskip("mpmath")
+    import hp_truth
+    p = plan(name)
+    inp = PINS["cases"][name]["input"]
+    ref = ol.Prepared(inp).samples(0, 0, N_REC)
+    rec = p.records(N_REC, seed=0, precision=ft.FP64)
+    err = sample_errors(rec, ref)
+    info = dict(p.info)
+    for i in np.argsort(-err)[:3]:
+        t = np.array(hp_truth.truth(inp, info, ref["X"][i], ref["psi_tr"][i], ref["xi_tr"][i]))
+        scale = np.abs(t).max()
+        gpu = np.abs(rec["R"][i] - t).max() / scale
+        cpu = np.abs(ref["R"][i] - t).max() / scale
+        print(name, i, "vs 50 digits: gpu %.1e oracle %.1e" % (gpu, cpu))
+        assert gpu < 1e-9
 
 
 def test_skip_ahead_matches_stream_order():
