@@ -22,10 +22,12 @@ static const char* kArch = "--gpu-architecture=sm_103a";
 
 unsigned table_smem_bytes(const kernel_key& k)
 {
-    if (k.table_global) return 0;
+    // staged table (unless read from global memory), then the per-thread accumulators
     const unsigned entries = 1u << k.E;
-    const unsigned b = k.prec == 0 ? 25u * entries : 13u * entries;
-    return (b + 15u) & ~15u;
+    const unsigned tab = k.table_global ? 0u : (k.prec == 0 ? 25u * entries : 13u * entries);
+    const unsigned parts = k.mode == 1 ? 4u : 2u;
+    const unsigned acc = (unsigned)k.block * parts * (unsigned)k.K * (k.prec == 0 ? 16u : 24u);
+    return ((tab + 15u) & ~15u) + acc;
 }
 
 std::string kernel_source(const kernel_key& k)
@@ -37,6 +39,7 @@ std::string kernel_source(const kernel_key& k)
     s << "#define FT_PREC " << k.prec << "\n#define FT_MODE " << k.mode << "\n";
     s << "#define FT_ONLY_PSI " << k.only_psi << "\n#define FT_RECORD " << k.record << "\n";
     s << "#define FT_BLOCK " << k.block << "\n#define FT_TABLE_GLOBAL " << k.table_global << "\n";
+    s << "#define FT_MINB " << k.minb << "\n";
     s << "__device__ constexpr int FT_EK[" << k.E << "] = {";
     for (int e = 0; e < k.E; e++) s << (e ? "," : "") << k.ek[e];
     s << "};\n__device__ constexpr int FT_EL[" << k.E << "] = {";
@@ -183,7 +186,7 @@ static std::string key_string(const kernel_key& k)
 {
     std::ostringstream s;
     s << k.E << "," << k.V << "," << k.K << "," << k.loops << "," << k.rank << "," << k.prec << "," << k.mode << ","
-      << k.only_psi << "," << k.record << "," << k.block << "," << k.table_global;
+      << k.only_psi << "," << k.record << "," << k.block << "," << k.table_global << "," << k.minb;
     for (int e = 0; e < k.E; e++) s << ";" << k.ek[e] << "-" << k.el[e];
     return s.str();
 }

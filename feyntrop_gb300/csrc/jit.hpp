@@ -22,6 +22,7 @@ struct kernel_key {
     int only_psi = 0;
     int record = 0;
     int block = 128;
+    int minb = 1;           // minimum resident blocks per SM asked of the register allocator
     std::vector<int> ek, el;
 };
 

@@ -43,6 +43,9 @@
 #ifndef FT_E
 #error "topology constants missing"
 #endif
+#ifndef FT_MINB
+#define FT_MINB 1
+#endif
 
 typedef unsigned long long u64;
 typedef unsigned int u32;
@@ -70,7 +73,8 @@ typedef unsigned int u32;
 #define P_SIG (8 + 2 * FT_E)
 #define P_Q (8 + 2 * FT_E + FT_RANK)
 #define P_SIZE (8 + 2 * FT_E + FT_RANK + FT_RANK * FT_N)
-// the same block as floats follows at prm + P_SIZE (mixed form reads only that)
+// the same block as floats follows at prm + P_SIZE, then as two-float (hi, lo) pairs at
+// prm + P_SIZE + (P_SIZE + 1) / 2 (the mixed form reads only those two)
 
 // ------------------------------------------------------------------ table layout
 // [w64 | Jr64 | rinv64 : 8 bytes each][meta : 1 byte][pad to 16][w32 | Jr32 | rinv32]
@@ -748,83 +752,182 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
 // ------------------------------------------------------------------ integrand, mixed
 #if FT_PREC == 1
 #if FT_MODE == 1
-// x-derivatives of phi/psi at the sample point (srcs/laplacian.hpp:102-215) and the
-// deformation angle theta = -lambda (d(phi/psi)/dx + m^2) (srcs/feynman_integral.hpp:290-291),
-// in FP64 from FP32 conductances; outputs theta and the upper triangle of H.
-static __device__ __forceinline__ void derivatives64(const float* Xi32, const double* prm, float* theta_out,
-                                                     float (*H_out)[FT_E])
+// ------------------------------------------------------------------ two-float arithmetic
+// Values hi + lo with |lo| <= ulp(hi)/2 (about 48 significant bits) from error-free
+// transformations of FP32 operations (Knuth's two-sum, the FMA two-product); they run
+// on the FP32 pipe, which is ~60x wider than the FP64 pipe on this GPU.
+struct df {
+    float hi, lo;
+};
+static __device__ __forceinline__ df df_mk(float x)
 {
-    double Xi[FT_E];
+    df r;
+    r.hi = x;
+    r.lo = 0.0f;
+    return r;
+}
+static __device__ __forceinline__ df df_norm(float s, float e)
+{
+    df r;
+    r.hi = s + e;
+    r.lo = e - (r.hi - s);
+    return r;
+}
+static __device__ __forceinline__ df df_add(df x, df y)
+{
+    const float s = x.hi + y.hi;
+    const float bb = s - x.hi;
+    float e = (x.hi - (s - bb)) + (y.hi - bb);
+    e += x.lo + y.lo;
+    return df_norm(s, e);
+}
+static __device__ __forceinline__ df df_neg(df x)
+{
+    x.hi = -x.hi;
+    x.lo = -x.lo;
+    return x;
+}
+static __device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
+static __device__ __forceinline__ df df_mul(df x, df y)
+{
+    const float p = x.hi * y.hi;
+    float e = fmaf(x.hi, y.hi, -p);
+    e = fmaf(x.hi, y.lo, e);
+    e = fmaf(x.lo, y.hi, e);
+    return df_norm(p, e);
+}
+static __device__ __forceinline__ df df_fma(df x, df y, df z) { return df_add(df_mul(x, y), z); }
+static __device__ __forceinline__ df df_inv(df x)
+{
+    // one Newton step from the FP32 reciprocal: r + r (1 - x r)
+    const float r = 1.0f / x.hi;
+    const df e = df_sub(df_mk(1.0f), df_mul(x, df_mk(r)));
+    return df_add(df_mk(r), df_mul(df_mk(r), e));
+}
+static __device__ __forceinline__ float df_f(df x) { return x.hi + x.lo; }
+
+// x-derivatives of phi/psi at the sample point (srcs/laplacian.hpp:102-215) and the
+// deformation angle theta = -lambda (d(phi/psi)/dx + m^2) (srcs/feynman_integral.hpp:290-291).
+// Everything here is a difference of entries of L^-1, which cancels in FP32 for a
+// sizeable fraction of sectors, so the block runs in two-float arithmetic: the
+// conductance-form elimination (all operations on positive values), G = L^-1, the
+// potentials h_r = G q_r and their drops across the edges, the effective-resistance
+// combinations t, and the Minkowski products s.  Outputs theta and the upper
+// triangle of H in FP32.  pd: the parameter block as two-float pairs.
+static __device__ __forceinline__ void derivatives_df(const float* Xi32, const float* pd, float* theta_out,
+                                                      float (*H_out)[FT_E])
+{
+    df c[FT_N][FT_N], g[FT_N];
 #pragma unroll
-    for (int e = 0; e < FT_E; e++) Xi[e] = (double)Xi32[e];
-    elim<double, double> L;
-    L.factor(Xi);
-    double Nm[FT_N][FT_N];
+    for (int i = 0; i < FT_N; i++) {
+        g[i] = df_mk(0.0f);
+#pragma unroll
+        for (int j = 0; j < FT_N; j++) c[i][j] = df_mk(0.0f);
+    }
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        const int k = FT_EK[e], l = FT_EL[e];
+        if (k == FT_V - 1)
+            g[l] = df_add(g[l], df_mk(Xi32[e]));
+        else
+            c[l][k] = df_add(c[l][k], df_mk(Xi32[e]));
+    }
+    df a[FT_N][FT_N], id[FT_N];
+#pragma unroll
+    for (int k = 0; k < FT_N; k++) {
+        df dk = g[k];
+#pragma unroll
+        for (int j = k + 1; j < FT_N; j++) dk = df_add(dk, c[k][j]);
+        id[k] = df_inv(dk);
+#pragma unroll
+        for (int i = k + 1; i < FT_N; i++) a[k][i] = df_mul(c[k][i], id[k]);
+#pragma unroll
+        for (int i = k + 1; i < FT_N; i++) {
+            g[i] = df_fma(a[k][i], g[k], g[i]);
+#pragma unroll
+            for (int j = i + 1; j < FT_N; j++) c[i][j] = df_fma(a[k][i], c[k][j], c[i][j]);
+        }
+    }
+    // N = M^-1 (unit upper triangular, non-negative), G = N diag(1/d) N^T
+    df Nm[FT_N][FT_N];
 #pragma unroll
     for (int i = FT_N - 1; i >= 0; i--) {
 #pragma unroll
-        for (int j = 0; j < FT_N; j++) Nm[i][j] = 0.0;
-        Nm[i][i] = 1.0;
-#pragma unroll
         for (int j = i + 1; j < FT_N; j++) {
-            double s = 0.0;
+            df s = a[i][j];
 #pragma unroll
-            for (int k = i + 1; k <= j; k++) s = fma(L.a[i][k], Nm[k][j], s);
+            for (int k = i + 1; k < j; k++) s = df_fma(a[i][k], Nm[k][j], s);
             Nm[i][j] = s;
         }
     }
-    double id[FT_N];
-#pragma unroll
-    for (int k = 0; k < FT_N; k++) id[k] = 1.0 / L.d[k];
-    double G[FT_N][FT_N];
+    df G[FT_N][FT_N];
 #pragma unroll
     for (int i = 0; i < FT_N; i++)
 #pragma unroll
         for (int j = i; j < FT_N; j++) {
-            double s = 0.0;
+            // k = j term has N[j][j] = 1
+            df s = (i == j) ? id[j] : df_mul(Nm[i][j], id[j]);
 #pragma unroll
-            for (int k = j; k < FT_N; k++) s = fma(Nm[i][k] * Nm[j][k], id[k], s);
+            for (int k = j + 1; k < FT_N; k++) s = df_fma(df_mul(Nm[i][k], Nm[j][k]), id[k], s);
             G[i][j] = s;
             G[j][i] = s;
         }
-    double hb[FT_RANK][FT_E];
+    df hb[FT_RANK][FT_E];
 #pragma unroll
     for (int r = 0; r < FT_RANK; r++) {
-        double h[FT_N];
+        df h[FT_N];
 #pragma unroll
         for (int i = 0; i < FT_N; i++) {
-            double s = 0.0;
+            df s = df_mk(0.0f);
 #pragma unroll
-            for (int j = 0; j < FT_N; j++) s = fma(G[i][j], prm[P_Q + r * FT_N + j], s);
+            for (int j = 0; j < FT_N; j++) {
+                df q;
+                q.hi = pd[2 * (P_Q + r * FT_N + j)];
+                q.lo = pd[2 * (P_Q + r * FT_N + j) + 1];
+                s = df_fma(G[i][j], q, s);
+            }
             h[i] = s;
         }
 #pragma unroll
         for (int e = 0; e < FT_E; e++) {
             const int k = FT_EK[e], l = FT_EL[e];
-            hb[r][e] = (k == FT_V - 1 ? 0.0 : h[k]) - h[l];
+            hb[r][e] = (k == FT_V - 1) ? df_neg(h[l]) : df_sub(h[k], h[l]);
         }
     }
-    auto Gx = [&](int i, int j) -> double { return (i == FT_V - 1 || j == FT_V - 1) ? 0.0 : G[i][j]; };
-    const double kappa = prm[P_DEF];
+    auto Gx = [&](int i, int j) -> df { return (i == FT_V - 1 || j == FT_V - 1) ? df_mk(0.0f) : G[i][j]; };
+    const float kappa = pd[2 * P_DEF];
 #pragma unroll
-    for (int a = 0; a < FT_E; a++) {
-        const int ka = FT_EK[a], la = FT_EL[a];
-        double s = 0.0;
+    for (int a2 = 0; a2 < FT_E; a2++) {
+        const int ka = FT_EK[a2], la = FT_EL[a2];
+        df sig_hb[FT_RANK];
+        df s = df_mk(0.0f);
 #pragma unroll
-        for (int r = 0; r < FT_RANK; r++) s = fma(prm[P_SIG + r] * hb[r][a], hb[r][a], s);
-        const double t = Gx(ka, ka) + Gx(la, la) - 2.0 * Gx(ka, la);
-        const double xa = Xi[a] * Xi[a];
-        const double xas = xa * s;
-        theta_out[a] = (float)((prm[P_M2 + a] - xas) * kappa);
-        H_out[a][a] = (float)(2.0 * xas * (Xi[a] - xa * t));
+        for (int r = 0; r < FT_RANK; r++) {
+            df sg;
+            sg.hi = pd[2 * (P_SIG + r)];
+            sg.lo = pd[2 * (P_SIG + r) + 1];
+            sig_hb[r] = df_mul(sg, hb[r][a2]);
+            s = df_fma(sig_hb[r], hb[r][a2], s);
+        }
+        const df t = df_sub(df_add(Gx(ka, ka), Gx(la, la)), df_add(Gx(ka, la), Gx(ka, la)));
+        const df xi = df_mk(Xi32[a2]);
+        const df xa = df_mul(xi, xi);
+        const df xas = df_mul(xa, s);
+        df m2;
+        m2.hi = pd[2 * (P_M2 + a2)];
+        m2.lo = pd[2 * (P_M2 + a2) + 1];
+        theta_out[a2] = df_f(df_sub(m2, xas)) * kappa;
+        // 2 xa s (1/x - xa t)
+        H_out[a2][a2] = 2.0f * df_f(df_mul(xas, df_sub(xi, df_mul(xa, t))));
 #pragma unroll
-        for (int b = a + 1; b < FT_E; b++) {
+        for (int b = a2 + 1; b < FT_E; b++) {
             const int kb = FT_EK[b], lb = FT_EL[b];
-            double s2 = 0.0;
+            df s2 = df_mk(0.0f);
 #pragma unroll
-            for (int r = 0; r < FT_RANK; r++) s2 = fma(prm[P_SIG + r] * hb[r][a], hb[r][b], s2);
-            const double t2 = Gx(ka, kb) + Gx(la, lb) - Gx(ka, lb) - Gx(la, kb);
-            H_out[a][b] = (float)(-2.0 * xa * (Xi[b] * Xi[b]) * s2 * t2);
+            for (int r = 0; r < FT_RANK; r++) s2 = df_fma(sig_hb[r], hb[r][b], s2);
+            const df t2 = df_sub(df_add(Gx(ka, kb), Gx(la, lb)), df_add(Gx(ka, lb), Gx(la, kb)));
+            const float xb = Xi32[b];
+            H_out[a2][b] = -2.0f * df_f(df_mul(xa, df_mk(xb * xb))) * df_f(s2) * df_f(t2);
         }
     }
 }
@@ -908,7 +1011,7 @@ static __device__ __forceinline__ float wrap_pi(float x, bool& edge)
     return r;
 }
 
-static __device__ __forceinline__ bool integrand32(const double* prm, const float* pf, const f2* lx, f2 lF, f2 lG,
+static __device__ __forceinline__ bool integrand32(const float* pd, const float* pf, const f2* lx, f2 lF, f2 lG,
                                                    cx<float>* out, bool& need64)
 {
     need64 = false;
@@ -994,7 +1097,7 @@ static __device__ __forceinline__ bool integrand32(const double* prm, const floa
     // which cancel in FP32 for a sizeable fraction of sectors; this block runs in FP64.
     float theta[FT_E];
     float H[FT_E][FT_E];
-    derivatives64(Xi, prm, theta, H);
+    derivatives_df(Xi, pd, theta, H);
     cx<float> cX[FT_E], cy[FT_E];
     float xnu = 0.0f, thsum = 0.0f;
 #pragma unroll
@@ -1226,10 +1329,12 @@ static __device__ __forceinline__ void skip_lanes(xo& g, u32 lane, const u64* __
 // ------------------------------------------------------------------ table staging
 // FP64 form: shared = [w64 | Jr64 | 1/r64 | meta] (25 bytes per entry, the global
 // layout's first sections).  Mixed form: shared = [w32 | Jr32 | 1/r32 | meta].
-#if FT_PREC == 0
-#define SM_BYTES (25u * T_ENTRIES)
+#if FT_TABLE_GLOBAL
+#define SM_USED 0u
+#elif FT_PREC == 0
+#define SM_USED (25u * T_ENTRIES)
 #else
-#define SM_BYTES (13u * T_ENTRIES)
+#define SM_USED (13u * T_ENTRIES)
 #endif
 static __device__ __forceinline__ void copy_bytes(unsigned char* dst, const unsigned char* __restrict__ src, u32 bytes)
 {
@@ -1276,29 +1381,65 @@ static __device__ __forceinline__ table_ref stage_table(unsigned char* sm, const
 }
 
 // ------------------------------------------------------------------ per-thread accumulators
+// Per-thread sums live in shared memory (slot-major, so a warp touches consecutive
+// words), which keeps them out of the register budget of the sampling code:
+//   FP64 form: Neumaier-compensated FP64 sums per sample.
+//   mixed form: Kahan-compensated FP32 sums per sample, folded into the FP64
+//   Neumaier sums every 256 samples.
+// Slots: 4 per eps order (re f, re f^2, im f, im f^2).
+#if FT_MODE == 0
+#define ACC_PARTS 2   // undeformed integrand: real parts only
+#else
+#define ACC_PARTS 4
+#endif
+#define ACC_NS (ACC_PARTS * FT_K)
+#if FT_PREC == 0
+#define ACC_BYTES_PER_THREAD (ACC_NS * 16)
+#else
+#define ACC_BYTES_PER_THREAD (ACC_NS * 24)
+#endif
+#define ACC_SMEM_OFFSET ((SM_USED + 15u) & ~15u)
+
 struct accum {
-    nsum S[4 * FT_K];   // re S1, re S2, im S1, im S2 per eps order
+    double* S;   // [slot][thread] sums
+    double* C;   // [slot][thread] Neumaier compensations
 #if FT_PREC == 1
-    float Sf[4 * FT_K], Cf[4 * FT_K];   // FP32 Kahan sums, folded into S every 64 samples
+    float* Sf;   // [slot][thread] FP32 Kahan sums
+    float* Cf;
     int since_fold;
     float keptf, droppedf, queuedf, exactf;   // counters below 2^24 between folds
 #endif
     double kept, dropped, queued, exact, robust;
 
-    __device__ __forceinline__ void init()
+    __device__ __forceinline__ void init(unsigned char* smem_acc)
     {
-#pragma unroll
-        for (int s = 0; s < 4 * FT_K; s++) {
-            S[s].s = S[s].c = 0.0;
+        const int t = threadIdx.x;
+        S = (double*)smem_acc + t;
+        C = S + ACC_NS * FT_BLOCK;
 #if FT_PREC == 1
-            Sf[s] = Cf[s] = 0.0f;
-#endif
-        }
-#if FT_PREC == 1
+        Sf = (float*)((double*)smem_acc + 2 * ACC_NS * FT_BLOCK) + t;
+        Cf = Sf + ACC_NS * FT_BLOCK;
         since_fold = 0;
         keptf = droppedf = queuedf = exactf = 0.0f;
 #endif
+#pragma unroll
+        for (int s = 0; s < ACC_NS; s++) {
+            S[s * FT_BLOCK] = 0.0;
+            C[s * FT_BLOCK] = 0.0;
+#if FT_PREC == 1
+            Sf[s * FT_BLOCK] = 0.0f;
+            Cf[s * FT_BLOCK] = 0.0f;
+#endif
+        }
         kept = dropped = queued = exact = robust = 0.0;
+    }
+
+    __device__ __forceinline__ void nadd(int slot, double v)
+    {
+        const double s = S[slot * FT_BLOCK];
+        const double t = s + v;
+        C[slot * FT_BLOCK] += (fabs(s) >= fabs(v)) ? ((s - t) + v) : ((v - t) + s);
+        S[slot * FT_BLOCK] = t;
     }
 
     __device__ __forceinline__ void add64(const cx<double>* R)
@@ -1307,10 +1448,12 @@ struct accum {
 #pragma unroll
         for (int j = 0; j < FT_K; j++) {
             if (FT_ONLY_PSI && j > 0) break;
-            S[4 * j + 0].add(R[j].re);
-            S[4 * j + 1].add(R[j].re * R[j].re);
-            S[4 * j + 2].add(R[j].im);
-            S[4 * j + 3].add(R[j].im * R[j].im);
+            nadd(ACC_PARTS * j + 0, R[j].re);
+            nadd(ACC_PARTS * j + 1, R[j].re * R[j].re);
+            if (ACC_PARTS == 4) {
+                nadd(ACC_PARTS * j + 2, R[j].im);
+                nadd(ACC_PARTS * j + 3, R[j].im * R[j].im);
+            }
         }
     }
 
@@ -1324,11 +1467,13 @@ struct accum {
             const float re = R[j].re, im = R[j].im;
             const float v[4] = {re, re * re, im, im * im};
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const float y = v[q] - Cf[4 * j + q];
-                const float tt = Sf[4 * j + q] + y;
-                Cf[4 * j + q] = (tt - Sf[4 * j + q]) - y;
-                Sf[4 * j + q] = tt;
+            for (int q = 0; q < ACC_PARTS; q++) {
+                const int o = (ACC_PARTS * j + q) * FT_BLOCK;
+                const float sf = Sf[o];
+                const float y = v[q] - Cf[o];
+                const float tt = sf + y;
+                Cf[o] = (tt - sf) - y;
+                Sf[o] = tt;
             }
         }
         if (++since_fold == 256) fold();
@@ -1343,9 +1488,10 @@ struct accum {
     {
         since_fold = 0;
 #pragma unroll
-        for (int s = 0; s < 4 * FT_K; s++) {
-            S[s].add((double)Sf[s] - (double)Cf[s]);
-            Sf[s] = Cf[s] = 0.0f;
+        for (int s = 0; s < ACC_NS; s++) {
+            nadd(s, (double)Sf[s * FT_BLOCK] - (double)Cf[s * FT_BLOCK]);
+            Sf[s * FT_BLOCK] = 0.0f;
+            Cf[s * FT_BLOCK] = 0.0f;
         }
         kept += keptf;
         dropped += droppedf;
@@ -1362,10 +1508,15 @@ struct accum {
 #endif
         double vals[ACC_SLOTS];
 #pragma unroll
-        for (int s = 0; s < 4 * FT_K; s++) {
-            const double h = S[s].s + S[s].c;
-            vals[2 * s] = h;
-            vals[2 * s + 1] = S[s].c - (h - S[s].s);
+        for (int s = 0; s < 8 * FT_K; s++) vals[s] = 0.0;
+#pragma unroll
+        for (int s = 0; s < ACC_NS; s++) {
+            const double sv = S[s * FT_BLOCK], cv = C[s * FT_BLOCK];
+            const double h = sv + cv;
+            // slot s = (order j, part q) -> output pair 4 j + q
+            const int o = 4 * (s / ACC_PARTS) + (s % ACC_PARTS);
+            vals[2 * o] = h;
+            vals[2 * o + 1] = cv - (h - sv);
         }
         vals[ACC_KEPT] = kept;
         vals[ACC_DROPPED] = dropped;
@@ -1428,7 +1579,7 @@ static __device__ __forceinline__ void sample64(xo& g, const table_ref& tr, cons
 // its partial sums to acc_out[b * ACC_SLOTS ...].  In the mixed form, samples whose
 // FP32 evaluation is not trustworthy are appended to `queue` (index and stream
 // state, 5 words) for the FP64 pass and left out of the sums here.
-extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample(
+extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
     const double* __restrict__ prm, const unsigned char* __restrict__ tab, const u64* __restrict__ lanepw,
     int lanebits, u64 s0, u64 s1, u64 s2, u64 s3, u64 nsamples, u64 chunk, double* __restrict__ acc_out,
     u64* __restrict__ queue, unsigned int* __restrict__ qcount, unsigned int qcap,
@@ -1441,6 +1592,7 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample(
     const u32 t = blockIdx.x * blockDim.x + threadIdx.x;
 #if FT_PREC == 1
     const float* pf = (const float*)(prm + P_SIZE);
+    const float* pd = (const float*)(prm + P_SIZE + (P_SIZE + 1) / 2);   // two-float pairs
 #endif
     xo g;
     g.a = s0;
@@ -1454,7 +1606,7 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample(
     if (last > nsamples) last = nsamples;
 
     accum A;
-    A.init();
+    A.init(smem + ACC_SMEM_OFFSET);
     for (u64 i = first; i < last; i++) {
 #if FT_PREC == 0
         sample64(g, tr, prm, i, A, 0, rec_order, rec_X, rec_R, rec_flags);
@@ -1471,7 +1623,7 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample(
         if (FT_RECORD)
             for (int e = 0; e < FT_E; e++) rec_X[i * FT_E + e] = exp((double)lx[e].hi + (double)lx[e].lo);
         bool need64 = false;
-        const bool ok = integrand32(prm, pf, lx, lF, lG, R, need64);
+        const bool ok = integrand32(pd, pf, lx, lF, lG, R, need64);
         if (need64) {
             flags |= REC_QUEUED;
             A.note32(0.0f, 1.0f, (float)ex);
@@ -1513,7 +1665,7 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue(
     unsigned int n = *qcount;
     if (n > qcap) n = qcap;
     accum A;
-    A.init();
+    A.init(smem + ACC_SMEM_OFFSET);
     for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
         const u64* q = queue + (size_t)k * 5;
         xo g;

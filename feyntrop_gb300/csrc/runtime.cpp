@@ -176,6 +176,10 @@ struct ft_plan {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;
+    // launch shape of the sampling kernels (threads per block, minimum resident blocks
+    // per SM given to the register allocator), from a sweep on GB300: the mixed form
+    // gains ~1.6x on deformed integrals from 256 x 2 (168 registers instead of 255)
+    int tuned_block = 256, tuned_minb = 2;
 
     ft::kernel_key key(int prec, int record) const
     {
@@ -189,12 +193,15 @@ struct ft_plan {
         k.mode = P.deformed() ? 1 : 0;
         k.only_psi = P.only_psi() ? 1 : 0;
         k.record = record;
-        k.block = 128;
+        k.block = tuned_block;
+        k.minb = prec == 0 ? 1 : tuned_minb;
+        if (const char* e = std::getenv("FEYNTROP_GB300_BLOCK")) k.block = std::atoi(e);
+        if (const char* e = std::getenv("FEYNTROP_GB300_MINB")) k.minb = std::atoi(e);
         k.ek = P.ek;
         k.el = P.el;
-        // stage the table in shared memory when it fits comfortably
-        const size_t bytes = (size_t)(prec == 0 ? 25 : 13) << P.E;
-        k.table_global = bytes > 160 * 1024 ? 1 : 0;
+        // small tables are staged per block in shared memory; from E = 11 on the table is
+        // read through L1 (one cached copy per SM instead of one per block)
+        k.table_global = P.E >= 11 ? 1 : 0;
         return k;
     }
 
@@ -264,10 +271,17 @@ void upload(ft_plan& pl)
 {
     cu(cudaGetDevice(&pl.device), "cudaGetDevice");
     // FP64 parameter block followed by the same values as floats
-    std::vector<double> blk(pl.prm.size() + (pl.prm.size() + 1) / 2, 0.0);
-    std::memcpy(blk.data(), pl.prm.data(), pl.prm.size() * 8);
-    float* f = (float*)(blk.data() + pl.prm.size());
-    for (size_t i = 0; i < pl.prm.size(); i++) f[i] = (float)pl.prm[i];
+    // FP64 block, then floats, then two-float (hi, lo) pairs
+    const size_t n = pl.prm.size();
+    std::vector<double> blk(n + (n + 1) / 2 + n, 0.0);
+    std::memcpy(blk.data(), pl.prm.data(), n * 8);
+    float* f = (float*)(blk.data() + n);
+    for (size_t i = 0; i < n; i++) f[i] = (float)pl.prm[i];
+    float* pd = (float*)(blk.data() + n + (n + 1) / 2);
+    for (size_t i = 0; i < n; i++) {
+        pd[2 * i] = (float)pl.prm[i];
+        pd[2 * i + 1] = (float)(pl.prm[i] - (double)pd[2 * i]);
+    }
     cu(cudaMalloc(&pl.d_prm, blk.size() * 8), "cudaMalloc(params)");
     cu(cudaMalloc(&pl.d_tab, pl.tab.size()), "cudaMalloc(table)");
     cu(cudaMemcpy(pl.d_prm, blk.data(), blk.size() * 8, cudaMemcpyHostToDevice), "cudaMemcpy(params)");
