@@ -814,7 +814,7 @@ static __device__ __forceinline__ float df_f(df x) { return x.hi + x.lo; }
 // potentials h_r = G q_r and their drops across the edges, the effective-resistance
 // combinations t, and the Minkowski products s.  Outputs theta and the upper
 // triangle of H in FP32.  pd: the parameter block as two-float pairs.
-static __device__ __forceinline__ void derivatives_df(const float* Xi32, const float* pd, float* theta_out,
+static __device__ __forceinline__ void derivatives_df(const float* Xi32, const float* pd, df* theta_out,
                                                       float (*H_out)[FT_E])
 {
     df c[FT_N][FT_N], g[FT_N];
@@ -916,7 +916,7 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
         df m2;
         m2.hi = pd[2 * (P_M2 + a2)];
         m2.lo = pd[2 * (P_M2 + a2) + 1];
-        theta_out[a2] = df_f(df_sub(m2, xas)) * kappa;
+        theta_out[a2] = df_mul(df_sub(m2, xas), df_mk(kappa));
         // 2 xa s (1/x - xa t)
         H_out[a2][a2] = 2.0f * df_f(df_mul(xas, df_sub(xi, df_mul(xa, t))));
 #pragma unroll
@@ -1011,6 +1011,17 @@ static __device__ __forceinline__ float wrap_pi(float x, bool& edge)
     return r;
 }
 
+// two-float variant of wrap_pi
+static __device__ __forceinline__ f2 wrap_pi2(f2 x, bool& edge)
+{
+    const float TWO_PI_HI = 6.28318548202514648f, TWO_PI_LO = -1.7484555e-7f;
+    const float k = rintf((x.hi + x.lo) * 0.159154943091895336f);
+    f2 r = f2_add(x, -k * TWO_PI_HI);
+    r = f2_add(r, -k * TWO_PI_LO);
+    edge |= fabsf(r.hi + r.lo) > 3.14158265f;
+    return r;
+}
+
 static __device__ __forceinline__ bool integrand32(const float* pd, const float* pf, const f2* lx, f2 lF, f2 lG,
                                                    cx<float>* out, bool& need64)
 {
@@ -1095,20 +1106,23 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     const float kappa = pf[P_DEF];
     // The contour (theta) and its Jacobian come from differences of entries of L^-1,
     // which cancel in FP32 for a sizeable fraction of sectors; this block runs in FP64.
-    float theta[FT_E];
+    df theta[FT_E];
     float H[FT_E][FT_E];
     derivatives_df(Xi, pd, theta, H);
     cx<float> cX[FT_E], cy[FT_E];
-    float xnu = 0.0f, thsum = 0.0f;
+    // phase sums in two-float: sum theta and nu . theta
+    f2 xnu = f2_make(0.0f, 0.0f), thsum = f2_make(0.0f, 0.0f);
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
-        FT_DBG(e, theta[e]);
+        FT_DBG(e, theta[e].hi + theta[e].lo);
         float sn, cs;
-        sincosf(theta[e], &sn, &cs);
-        cX[e] = cmk(X[e] * cs, X[e] * sn);
-        cy[e] = cmk(Xi[e] * cs, -Xi[e] * sn);
-        xnu = fmaf(pf[P_NU + e], theta[e], xnu);
-        thsum += theta[e];
+        sincosf(theta[e].hi, &sn, &cs);
+        // first-order correction for the low part: sin(h + l) = sin h + l cos h
+        const float cs2 = fmaf(-theta[e].lo, sn, cs), sn2 = fmaf(theta[e].lo, cs, sn);
+        cX[e] = cmk(X[e] * cs2, X[e] * sn2);
+        cy[e] = cmk(Xi[e] * cs2, -Xi[e] * sn2);   // 1 / cX
+        thsum = f2_add2(thsum, f2_make(theta[e].hi, theta[e].lo));
+        xnu = f2_add2(xnu, f2_mulf(f2_make(theta[e].hi, theta[e].lo), pf[P_NU + e]));
     }
     elim<cx<float>, float> CL;
     const float growth = CL.factor(cy);
@@ -1130,7 +1144,9 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
         ph = ph * cmk(CL.d[k].re * im, CL.d[k].im * im);
     }
     bool edge = false;
-    const float apsi = wrap_pi(thsum + atan2f(ph.im, ph.re), edge);
+    // arg cPsi = sum theta + arg det, reduced to the principal branch in two-float
+    const f2 apsi2 = wrap_pi2(f2_add(thsum, atan2f(ph.im, ph.re)), edge);
+    const float apsi = apsi2.hi + apsi2.lo;
     // phi/psi of the deformed point and the deformed V
     cx<float> cpphi = cmk(0.0f, 0.0f);
     float mag = 0.0f;
@@ -1206,10 +1222,19 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     f2 t = f2_add2(f2_mulf(lpsi, -D2), f2_mulf(lv, -W));
     t = f2_add(t, (float)mj.e);
     t = f2_add(t, log2f(mj.m));
-    const float ang = -D2 * apsi + atan2f(pj.im, pj.re) + xnu - W * av;
+    // arg cR = -D/2 arg cPsi + arg det J + nu . theta - W arg V (two-float sum)
+    f2 angf = f2_add2(f2_mulf(apsi2, -D2), xnu);
+    angf = f2_add(angf, atan2f(pj.im, pj.re));
+    angf = f2_add(angf, -W * av);
+    const float ang = angf.hi;
     const float mod = exp2f(t.hi) * (1.0f + t.lo * LN2_F);
     float sn, cs;
     sincosf(ang, &sn, &cs);
+    {
+        const float c2 = fmaf(-angf.lo, sn, cs), s2 = fmaf(angf.lo, cs, sn);
+        cs = c2;
+        sn = s2;
+    }
     if (!isfinite(mod)) {
         need64 = true;
         return false;
