@@ -34,7 +34,7 @@ MIXED = 1
 
 EXPORTED = ["ft_plan_create", "ft_plan_destroy", "ft_plan_get_info", "ft_plan_log_line", "ft_integrate",
             "ft_integrate_batch", "ft_finalize_moments", "ft_sample_records", "ft_run_json", "ft_free",
-            "ft_precompile", "ft_last_error", "ft_version", "ft_subgraph_table", "ft_device_peaks"]
+            "ft_precompile", "ft_last_error", "ft_version", "ft_subgraph_table", "ft_device_peaks", "ft_integrate_noalloc"]
 
 
 class FeyntropError(RuntimeError):
@@ -105,6 +105,7 @@ def lib():
                                       ctypes.POINTER(ctypes.c_void_p)]
             L.ft_free.argtypes = [ctypes.c_void_p]
             L.ft_precompile.argtypes = [ctypes.POINTER(Problem), ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
+            L.ft_integrate_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(RunOptions), ctypes.c_void_p]
             L.ft_device_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             L.ft_subgraph_table.argtypes = [ctypes.POINTER(Problem)] + [ctypes.c_void_p] * 4 + [
                 ctypes.POINTER(PlanInfo)]

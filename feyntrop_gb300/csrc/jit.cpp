@@ -191,10 +191,22 @@ static std::string key_string(const kernel_key& k)
     return s.str();
 }
 
+static std::mutex g_mu;
+static std::map<std::pair<int, std::string>, kernel_set> g_loaded;
+
+const kernel_set* find_kernels(const kernel_key& key)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_loaded.find(std::make_pair(dev, key_string(key)));
+    return it == g_loaded.end() ? nullptr : &it->second;
+}
+
 const kernel_set& get_kernels(const kernel_key& key)
 {
-    static std::mutex mu;
-    static std::map<std::pair<int, std::string>, kernel_set> loaded;
+    auto& mu = g_mu;
+    auto& loaded = g_loaded;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) throw std::runtime_error("no CUDA device");
     std::lock_guard<std::mutex> lock(mu);

@@ -60,6 +60,9 @@ void check(CUresult r, const char* what);
 // compiled and loaded on the current device (throws std::runtime_error)
 const kernel_set& get_kernels(const kernel_key& key);
 
+// already loaded on the current device, else nullptr (never compiles or loads)
+const kernel_set* find_kernels(const kernel_key& key);
+
 // compile only (no device needed); returns the cubin size
 size_t compile_only(const kernel_key& key, std::string* log = nullptr);
 

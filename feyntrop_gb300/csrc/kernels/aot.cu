@@ -9,6 +9,8 @@
 //                      the counters.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "aot.hpp"
 
 typedef unsigned long long u64;
@@ -151,6 +153,47 @@ double fma_peak_tflops(bool fp64)
     cudaFree(buf);
     const double flops = 2.0 * 8 * (double)iters * blocks * 256;
     return flops / (best * 1e-3) / 1e12;
+}
+
+// ------------------------------------------------------------------ no-allocation scratch
+// Scratch of ft_integrate_noalloc, for callers that must not allocate device memory
+// during an integration.  It is one file-scope device array per GPU that loads this
+// library, held until the process exits:
+//   [2 words] FP64 hand-off queue count, [NOALLOC_PART_DOUBLES] per-block partial
+//   moments, [5 * NOALLOC_QUEUE_ENTRIES] hand-off queue, [NOALLOC_LANE_WORDS] lane
+//   skip matrices.
+// Every call shares it (and it keeps the last call's contents), so calls that overlap
+// on the GPU race; the queue count is cleared at the start of each call.
+static __device__ __align__(256) u64 g_noalloc_scratch[NOALLOC_TOTAL_WORDS];
+
+cudaError_t noalloc_scratch(noalloc_layout* out)
+{
+    // In host code g_noalloc_scratch names a host-side stand-in; the device address is
+    // looked up once per device, with that device current.
+    static std::mutex mu;
+    static void* addr[64] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    void* base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!addr[dev]) {
+            e = cudaGetSymbolAddress(&addr[dev], g_noalloc_scratch);
+            if (e != cudaSuccess) {
+                addr[dev] = nullptr;
+                return e;
+            }
+        }
+        base = addr[dev];
+    }
+    u64* w = (u64*)base;
+    out->qcount = (unsigned int*)w;
+    out->parts = (double*)(w + 2);
+    out->queue = w + 2 + NOALLOC_PART_DOUBLES;
+    out->lanepw = w + 2 + NOALLOC_PART_DOUBLES + 5 * (size_t)NOALLOC_QUEUE_ENTRIES;
+    return cudaSuccess;
 }
 
 cudaError_t launch_lane_powers(const u64* tpow, u64 S, int nbits, u64* out, cudaStream_t st)

@@ -12,6 +12,28 @@ cudaError_t launch_lane_powers(const unsigned long long* tpow, unsigned long lon
 // out[s] = sum over parts of parts[p * slots + s]; slots [0, ndd) are (hi, lo) pairs
 cudaError_t launch_finalize(const double* parts, int nparts, int slots, int ndd, double* out, cudaStream_t st);
 
+// Limits of the no-allocation path (ft_integrate_noalloc): per-block partial moments
+// for up to 2048 blocks of up to 136 slots (16 eps orders), 65536 FP64 hand-off
+// entries, lane skip matrices for up to 2^24 lanes.  About 5 MB per device.
+#define NOALLOC_MAX_BLOCKS 2048
+#define NOALLOC_MAX_SLOTS 136
+#define NOALLOC_PART_DOUBLES (NOALLOC_MAX_BLOCKS * NOALLOC_MAX_SLOTS)
+#define NOALLOC_QUEUE_ENTRIES 65536
+#define NOALLOC_MAX_LANE_BITS 24
+#define NOALLOC_LANE_WORDS (NOALLOC_MAX_LANE_BITS * 1024)
+#define NOALLOC_TOTAL_WORDS (2 + NOALLOC_PART_DOUBLES + 5 * NOALLOC_QUEUE_ENTRIES + NOALLOC_LANE_WORDS)
+
+struct noalloc_layout {
+    unsigned int* qcount;
+    double* parts;
+    unsigned long long* queue;
+    unsigned long long* lanepw;
+};
+
+// device addresses inside the static scratch of the current device (first call per
+// device looks the symbol up)
+cudaError_t noalloc_scratch(noalloc_layout* out);
+
 // FMA issue-rate probe (TFLOP/s, FMA = 2 flops) of the current device
 double fma_peak_tflops(bool fp64);
 

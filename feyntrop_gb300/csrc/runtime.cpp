@@ -655,6 +655,70 @@ int ft_integrate_batch(ft_plan* const* plans, int32_t count, const ft_run_option
     return FT_OK;
 }
 
+int ft_integrate_noalloc(ft_plan* pl, const ft_run_options* o, double* d_slots)
+{
+    try {
+        std::lock_guard<std::mutex> lock(pl->mu);
+        cu(cudaSetDevice(pl->device), "cudaSetDevice");
+        if (!d_slots) throw std::invalid_argument("ft_integrate_noalloc: output pointer is NULL");
+        const int prec = o->precision == FT_PRECISION_MIXED ? 1 : 0;
+        if (pl->slots() > NOALLOC_MAX_SLOTS)
+            throw std::invalid_argument("ft_integrate_noalloc: more than 16 eps orders exceed the static scratch");
+        const ft::kernel_set* ks = ft::find_kernels(pl->key(prec, 0));
+        const ft::kernel_set* k64 = prec ? ft::find_kernels(pl->key(0, 0)) : nullptr;
+        if (!ks || (prec && !k64))
+            throw std::invalid_argument(
+                "ft_integrate_noalloc: this plan's kernels are not loaded; call ft_integrate once with the same "
+                "precision first (loading them allocates)");
+        const unsigned long long N = o->num_samples;
+        if (N == 0) throw std::invalid_argument("ft_integrate_noalloc: num_samples must be positive");
+        const launch_geometry g = geometry(*ks, N);
+        const unsigned qblocks = prec ? (unsigned)(dev_state().sms * std::max(1, k64->queue_blocks_per_sm)) : 0;
+        if (g.blocks + qblocks > NOALLOC_MAX_BLOCKS || g.lanebits > NOALLOC_MAX_LANE_BITS)
+            throw std::invalid_argument("ft_integrate_noalloc: launch exceeds the static scratch (2048 blocks)");
+        ft::noalloc_layout sc;
+        cu(ft::noalloc_scratch(&sc), "cudaGetSymbolAddress(no-allocation scratch)");
+        cudaStream_t st = o->stream ? (cudaStream_t)o->stream : pl->stream;
+        const unsigned long long draws = 2ULL * pl->P.E - 1;
+        cu(ft::launch_lane_powers(dev_state().tpow, g.chunk * draws, g.lanebits, sc.lanepw, st), "lane skip matrices");
+        cu(cudaMemsetAsync(sc.qcount, 0, 8, st), "cudaMemsetAsync");
+        const ft::xstate base = ft::advance(ft::seed_state(o->seed), o->first_sample * draws);
+        unsigned long long s0 = base.s[0], s1 = base.s[1], s2 = base.s[2], s3 = base.s[3];
+        unsigned long long nsamples = N, chunk = g.chunk;
+        int lanebits = g.lanebits;
+        unsigned int qcap = NOALLOC_QUEUE_ENTRIES;
+        unsigned long long* queue = sc.queue;
+        unsigned int* qcount = sc.qcount;
+        double* parts = sc.parts;
+        const double* prm = pl->d_prm;
+        const unsigned char* tab = pl->d_tab;
+        const unsigned long long* lanepw = sc.lanepw;
+        uint8_t* r_order = nullptr;
+        double* r_X = nullptr;
+        double* r_R = nullptr;
+        uint8_t* r_flags = nullptr;
+        void* args[] = {&prm, &tab, &lanepw, &lanebits, &s0, &s1, &s2, &s3, &nsamples, &chunk, &parts, &queue, &qcount,
+                        &qcap, &r_order, &r_X, &r_R, &r_flags};
+        ft::check(ft::drv().LaunchKernel(ks->sample, g.blocks, 1, 1, ks->block, 1, 1, ks->smem, (CUstream)st, args,
+                                         nullptr),
+                  "launch ft_sample");
+        if (prec) {
+            double* qparts = sc.parts + (size_t)g.blocks * pl->slots();
+            const unsigned long long* cq = sc.queue;
+            const unsigned int* cqc = sc.qcount;
+            void* qargs[] = {&prm, &tab, &cq, &cqc, &qcap, &qparts, &r_order, &r_X, &r_R, &r_flags};
+            ft::check(ft::drv().LaunchKernel(k64->queue, qblocks, 1, 1, k64->block, 1, 1, k64->smem, (CUstream)st,
+                                             qargs, nullptr),
+                      "launch ft_sample_queue");
+        }
+        cu(ft::launch_finalize(sc.parts, (int)(g.blocks + qblocks), pl->slots(), 8 * pl->P.K, d_slots, st),
+           "finalize");
+        return FT_OK;
+    } catch (...) {
+        return status_of(std::current_exception());
+    }
+}
+
 int ft_sample_records(ft_plan* pl, const ft_run_options* o, uint8_t* order, double* X, double* R, uint8_t* flags)
 {
     try {

@@ -112,6 +112,22 @@ int ft_integrate(ft_plan* plan, const ft_run_options* opts, ft_result* result);
 /* Several plans in one call (one launch per plan today, all on one stream). */
 int ft_integrate_batch(ft_plan* const* plans, int32_t count, const ft_run_options* opts, ft_result* results);
 
+/* Integration that allocates no memory, for callers that must not allocate device
+ * memory while they integrate (an embedding application or serving loop that owns all
+ * device memory, or a region where allocation is forbidden).  No counterpart in the
+ * reference.  Same samples and the same launches as ft_integrate, asynchronous on
+ * opts->stream (or the plan's stream): the final sums are written to d_slots, a
+ * caller-owned DEVICE buffer of 8K+8 doubles: for eps order j and part p (0 Re, 1 Im)
+ * [8j+4p .. +3] = sum f (hi, lo), sum f^2 (hi, lo); then kept, dropped, FP64
+ * re-evaluated, exact sector steps, complete-pivoting factorisations.
+ * Scratch is one static device array per GPU (about 5 MB, held until exit): at most
+ * 2048 blocks, 16 eps orders and 65536 samples handed to the FP64 pass per call (more
+ * are not evaluated: kept + dropped < N reports it).  The plan's kernels must already be
+ * loaded by one ft_integrate call with the same precision.  The first call on a device
+ * looks up the scratch address (call it once before any stream capture).  Calls share
+ * the scratch, so calls that overlap on the GPU race. */
+int ft_integrate_noalloc(ft_plan* plan, const ft_run_options* opts, double* d_slots);
+
 /* avg / acc from merged moments, with the reference's formulas (srcs/stats.hpp:86-104);
  * real_only marks integrals whose imaginary part the reference reports as (0, 0). */
 int ft_finalize_moments(const ft_moments* moments, int32_t num_eps_terms, int32_t real_only, ft_result* result);
