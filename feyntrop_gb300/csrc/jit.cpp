@@ -39,7 +39,7 @@ std::string kernel_source(const kernel_key& k)
     s << "#define FT_PREC " << k.prec << "\n#define FT_MODE " << k.mode << "\n";
     s << "#define FT_ONLY_PSI " << k.only_psi << "\n#define FT_RECORD " << k.record << "\n";
     s << "#define FT_BLOCK " << k.block << "\n#define FT_TABLE_GLOBAL " << k.table_global << "\n";
-    s << "#define FT_MINB " << k.minb << "\n";
+    s << "#define FT_MINB " << k.minb << "\n#define FT_VARIANT " << k.variant << "\n";
     s << "__device__ constexpr int FT_EK[" << k.E << "] = {";
     for (int e = 0; e < k.E; e++) s << (e ? "," : "") << k.ek[e];
     s << "};\n__device__ constexpr int FT_EL[" << k.E << "] = {";
@@ -186,7 +186,7 @@ static std::string key_string(const kernel_key& k)
 {
     std::ostringstream s;
     s << k.E << "," << k.V << "," << k.K << "," << k.loops << "," << k.rank << "," << k.prec << "," << k.mode << ","
-      << k.only_psi << "," << k.record << "," << k.block << "," << k.table_global << "," << k.minb;
+      << k.only_psi << "," << k.record << "," << k.block << "," << k.table_global << "," << k.minb << "," << k.variant;
     for (int e = 0; e < k.E; e++) s << ";" << k.ek[e] << "-" << k.el[e];
     return s.str();
 }

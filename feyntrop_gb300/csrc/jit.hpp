@@ -23,6 +23,7 @@ struct kernel_key {
     int record = 0;
     int block = 128;
     int minb = 1;           // minimum resident blocks per SM asked of the register allocator
+    int variant = 0;        // code-size options of the kernel body (FT_VARIANT)
     std::vector<int> ek, el;
 };
 

@@ -55,6 +55,32 @@ typedef unsigned int u32;
 #define FT_DBG(slot, value)
 #endif
 
+// Code size: the per-topology kernel is straight-line code (every loop unrolled so
+// that the small matrices stay in registers), and the FP32 library functions carry
+// large slow paths.  FT_VARIANT bit 0 keeps one out-of-line copy of each FP32
+// transcendental, bit 1 does the same for the two-float primitives, so the code the
+// SM streams per sample fits the instruction caches better.
+#ifndef FT_VARIANT
+#define FT_VARIANT 0
+#endif
+#if (FT_VARIANT & 1) && !defined(FT_HOST_SIM)
+#define FT_MATHFN __noinline__
+#else
+#define FT_MATHFN __forceinline__
+#endif
+#if (FT_VARIANT & 2) && !defined(FT_HOST_SIM)
+#define FT_DFFN __noinline__
+#else
+#define FT_DFFN __forceinline__
+#endif
+static __device__ FT_MATHFN float m_log1p(float x) { return log1pf(x); }
+static __device__ FT_MATHFN float m_exp(float x) { return expf(x); }
+static __device__ FT_MATHFN float m_exp2(float x) { return exp2f(x); }
+static __device__ FT_MATHFN float m_log2(float x) { return log2f(x); }
+static __device__ FT_MATHFN float m_atan2(float y, float x) { return atan2f(y, x); }
+static __device__ FT_MATHFN float m_hypot(float x, float y) { return hypotf(x, y); }
+static __device__ FT_MATHFN void m_sincos(float x, float* s, float* c) { sincosf(x, s, c); }
+
 #define FT_N (FT_V - 1)
 #define FT_FULL ((1u << FT_E) - 1u)
 #define FT_NPAIR (FT_E * (FT_E - 1) / 2)
@@ -149,17 +175,28 @@ static __device__ __forceinline__ cx<T> operator*(cx<T> a, cx<T> b)
 }
 template <class T>
 static __device__ __forceinline__ cx<T> operator*(T s, cx<T> a) { return cmk(s * a.re, s * a.im); }
+// reciprocals: IEEE division in FP64; the correctly rounded reciprocal instruction
+// sequence in FP32 (a division there expands to a long inline sequence)
+static __device__ __forceinline__ double rcp_(double x) { return 1.0 / x; }
+#ifdef FT_HOST_SIM
+static __device__ __forceinline__ float rcp_(float x) { return 1.0f / x; }
+#else
+static __device__ __forceinline__ float rcp_(float x) { return __frcp_rn(x); }
+#endif
 template <class T>
 static __device__ __forceinline__ cx<T> crecip(cx<T> z)
 {
     // scaled so that |z|^2 cannot overflow in single precision
-    T s = fmax(fabs(z.re), fabs(z.im));
-    T r = z.re / s, i = z.im / s;
-    T d = s * (r * r + i * i);
-    return cmk(r / d, -i / d);
+    const T s = fmax(fabs(z.re), fabs(z.im));
+    const T is = rcp_(s);
+    const T r = z.re * is, i = z.im * is;
+    const T id = rcp_(s * (r * r + i * i));
+    return cmk(r * id, -i * id);
 }
 static __device__ __forceinline__ double cabs_(cx<double> z) { return hypot(z.re, z.im); }
-static __device__ __forceinline__ float cabs_(cx<float> z) { return hypotf(z.re, z.im); }
+// |z| for the pivots and determinants of the FP32 path (moduli far inside the
+// float range there: conductances 1/x of a sector stay below ~1e18)
+static __device__ __forceinline__ float cabs_(cx<float> z) { return sqrtf(fmaf(z.re, z.re, z.im * z.im)); }
 static __device__ __forceinline__ bool cfinite(cx<double> z) { return isfinite(z.re) && isfinite(z.im); }
 static __device__ __forceinline__ bool cfinite(cx<float> z) { return isfinite(z.re) && isfinite(z.im); }
 
@@ -220,7 +257,7 @@ struct elim {
                 mag += mag_of(c[k][j]);
             }
             d[k] = dk;
-            R ratio = mag_of(dk) / mag;
+            R ratio = mag_of(dk) * rcp_(mag);
             worst = ratio < worst ? ratio : worst;
             F inv = inv_of(dk);
 #pragma unroll
@@ -254,7 +291,7 @@ struct elim {
 
     static __device__ __forceinline__ R mag_of(R x) { return fabs(x); }
     static __device__ __forceinline__ R mag_of(cx<R> x) { return fabs(x.re) + fabs(x.im); }
-    static __device__ __forceinline__ R inv_of(R x) { return R(1) / x; }
+    static __device__ __forceinline__ R inv_of(R x) { return rcp_(x); }
     static __device__ __forceinline__ cx<R> inv_of(cx<R> x) { return crecip(x); }
     static __device__ __forceinline__ F from_real(R x)
     {
@@ -447,7 +484,7 @@ static __device__ __forceinline__ f2 log1m_u(u64 x)
     r.lo = 0.0f;
     if (m < (1ull << 52)) {
         // u < 1/2: log1p(-u)
-        r.hi = m ? log1pf(-__int_as_float(float_bits_of(m, -53))) : 0.0f;
+        r.hi = m ? m_log1p(-__int_as_float(float_bits_of(m, -53))) : 0.0f;
         return r;
     }
     // 1 - u = q 2^-53 exactly (q < 2^52); q = 2^k (1 + f): log(1 - u) = (k - 53) ln2 + log1p(f)
@@ -460,7 +497,27 @@ static __device__ __forceinline__ f2 log1m_u(u64 x)
     f2 a;
     a.hi = kk * LN2_HI;
     a.lo = kk * LN2_LO;
-    return f2_add(a, log1pf(f));
+    return f2_add(a, m_log1p(f));
+}
+
+// The reference's comparison, exactly (FP64, ascending edges, first running sum above
+// u * Jr(gamma), else the last edge): used when an FP32 comparison is within its
+// error margin.  Out of line: it runs for a few steps per 1e4 samples.
+static __device__ __noinline__ int exact_cut(u64 x, u32 sub, const unsigned char* __restrict__ gm)
+{
+    const double* w64 = (const double*)(gm + T_W64);
+    const double* Jr64 = (const double*)(gm + T_JR64);
+    const double R = u01(x) * Jr64[sub];
+    double TT = 0.0;
+    int cut = 0;
+    for (int c = 0; c < FT_E; c++) {
+        if ((sub >> c) & 1u) {
+            TT += w64[sub ^ (1u << c)];
+            cut = c;
+            if (TT > R) break;
+        }
+    }
+    return cut;
 }
 
 static __device__ __forceinline__ int draw_sector32(xo& g, const table_ref& t, const float* pf, f2* lx, f2& lF,
@@ -502,19 +559,7 @@ static __device__ __forceinline__ int draw_sector32(xo& g, const table_ref& t, c
         }
         int cut = sure >= 0 ? sure : e;
         if (unsure) {
-            // repeat the comparison exactly as the reference does it, in FP64
-            const double* w64 = (const double*)(t.gm + T_W64);
-            const double* Jr64 = (const double*)(t.gm + T_JR64);
-            const double R = u01(x) * Jr64[sub];
-            double TT = 0.0;
-            bool found = false;
-            for (int c = 0; c < FT_E; c++) {
-                if (((sub >> c) & 1u) && !found) {
-                    TT += w64[sub ^ (1u << c)];
-                    cut = c;
-                    found = TT > R;
-                }
-            }
+            cut = exact_cut(x, sub, t.gm);
             exact++;
         }
         sub ^= 1u << cut;
@@ -773,7 +818,7 @@ static __device__ __forceinline__ df df_norm(float s, float e)
     r.lo = e - (r.hi - s);
     return r;
 }
-static __device__ __forceinline__ df df_add(df x, df y)
+static __device__ FT_DFFN df df_add(df x, df y)
 {
     const float s = x.hi + y.hi;
     const float bb = s - x.hi;
@@ -788,7 +833,7 @@ static __device__ __forceinline__ df df_neg(df x)
     return x;
 }
 static __device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
-static __device__ __forceinline__ df df_mul(df x, df y)
+static __device__ FT_DFFN df df_mul(df x, df y)
 {
     const float p = x.hi * y.hi;
     float e = fmaf(x.hi, y.hi, -p);
@@ -797,10 +842,10 @@ static __device__ __forceinline__ df df_mul(df x, df y)
     return df_norm(p, e);
 }
 static __device__ __forceinline__ df df_fma(df x, df y, df z) { return df_add(df_mul(x, y), z); }
-static __device__ __forceinline__ df df_inv(df x)
+static __device__ FT_DFFN df df_inv(df x)
 {
     // one Newton step from the FP32 reciprocal: r + r (1 - x r)
-    const float r = 1.0f / x.hi;
+    const float r = rcp_(x.hi);
     const df e = df_sub(df_mk(1.0f), df_mul(x, df_mk(r)));
     return df_add(df_mk(r), df_mul(df_mk(r), e));
 }
@@ -996,7 +1041,7 @@ static __device__ __forceinline__ f2 log2_ratio(const mexp& mx, f2 lref)
 {
     f2 r = f2_mul2(lref, f2_make(RLN2_HI, RLN2_LO));
     r = f2_add(f2_neg(r), (float)mx.e);
-    return f2_add(r, log2f(mx.m));
+    return f2_add(r, m_log2(mx.m));
 }
 
 // principal argument reduced to (-pi, pi]; `edge` reports a value within 1e-5 of
@@ -1037,7 +1082,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
         const f2 a = f2_add(lx[e], -sh);
-        const float ep = expf(a.hi), em = expf(-a.hi);
+        const float ep = m_exp(a.hi), em = m_exp(-a.hi);
         X[e] = fmaf(ep, a.lo, ep);
         Xi[e] = fmaf(em, -a.lo, em);
     }
@@ -1059,7 +1104,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     const f2 lpsi = log2_ratio(psi, lFs);   // log2(psi / psi_tr)
 #if FT_ONLY_PSI
     const f2 t = f2_mulf(lpsi, -D2);
-    const float R = exp2f(t.hi) * (1.0f + t.lo * LN2_F);
+    const float R = m_exp2(t.hi) * (1.0f + t.lo * LN2_F);
     out[0] = cmk(IGtr * R, 0.0f);
     return true;
 #else
@@ -1085,7 +1130,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     mx_mul(V, pxi);
     const f2 lv = log2_ratio(V, lGs);   // log2(V / V_tr)
     const f2 t = f2_add2(f2_mulf(lpsi, -D2), f2_mulf(lv, -W));
-    const float Rf = exp2f(t.hi) * (1.0f + t.lo * LN2_F);
+    const float Rf = m_exp2(t.hi) * (1.0f + t.lo * LN2_F);
     if (!isfinite(Rf) || V.bad) {
         need64 = true;
         return false;
@@ -1093,10 +1138,10 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     float R = IGtr * Rf;
     out[0] = cmk(R, 0.0f);
     if (FT_K > 1) {
-        const float ef = LN2_F * ((float)(psi.e - FT_LOOPS * V.e) + (log2f(psi.m) - (float)FT_LOOPS * log2f(V.m)));
+        const float ef = LN2_F * ((float)(psi.e - FT_LOOPS * V.e) + (m_log2(psi.m) - (float)FT_LOOPS * m_log2(V.m)));
 #pragma unroll
         for (int j = 1; j < FT_K; j++) {
-            R *= ef / (float)j;
+            R *= ef * (1.0f / (float)j);
             out[j] = cmk(R, 0.0f);
         }
     }
@@ -1116,7 +1161,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     for (int e = 0; e < FT_E; e++) {
         FT_DBG(e, theta[e].hi + theta[e].lo);
         float sn, cs;
-        sincosf(theta[e].hi, &sn, &cs);
+        m_sincos(theta[e].hi, &sn, &cs);
         // first-order correction for the low part: sin(h + l) = sin h + l cos h
         const float cs2 = fmaf(-theta[e].lo, sn, cs), sn2 = fmaf(theta[e].lo, cs, sn);
         cX[e] = cmk(X[e] * cs2, X[e] * sn2);
@@ -1140,12 +1185,12 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     for (int k = 0; k < FT_N; k++) {
         const float m = cabs_(CL.d[k]);
         mx_mul(cpsi, m);
-        const float im = 1.0f / m;
+        const float im = rcp_(m);
         ph = ph * cmk(CL.d[k].re * im, CL.d[k].im * im);
     }
     bool edge = false;
     // arg cPsi = sum theta + arg det, reduced to the principal branch in two-float
-    const f2 apsi2 = wrap_pi2(f2_add(thsum, atan2f(ph.im, ph.re)), edge);
+    const f2 apsi2 = wrap_pi2(f2_add(thsum, m_atan2(ph.im, ph.re)), edge);
     const float apsi = apsi2.hi + apsi2.lo;
     // phi/psi of the deformed point and the deformed V
     cx<float> cpphi = cmk(0.0f, 0.0f);
@@ -1175,7 +1220,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     }
     mexp mv = mx_one();
     mx_mul(mv, vabs);
-    const float av = atan2f(cV.im, cV.re);
+    const float av = m_atan2(cV.im, cV.re);
     edge |= fabsf(av) > 3.14158265f;
     // det(I + i kappa X^1/2 H X^1/2)
     cx<float> J[FT_E][FT_E];
@@ -1198,7 +1243,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
         for (int j = k + 1; j < FT_E; j++) row += fabsf(J[k][j].re) + fabsf(J[k][j].im);
         jgrowth = fminf(jgrowth, m / row);
         mx_mul(mj, m);
-        const float im = 1.0f / m;
+        const float im = rcp_(m);
         pj = pj * cmk(piv.re * im, piv.im * im);
         const cx<float> inv = crecip(piv);
 #pragma unroll
@@ -1221,15 +1266,15 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     const f2 lv = log2_ratio(mv, lGs);
     f2 t = f2_add2(f2_mulf(lpsi, -D2), f2_mulf(lv, -W));
     t = f2_add(t, (float)mj.e);
-    t = f2_add(t, log2f(mj.m));
+    t = f2_add(t, m_log2(mj.m));
     // arg cR = -D/2 arg cPsi + arg det J + nu . theta - W arg V (two-float sum)
     f2 angf = f2_add2(f2_mulf(apsi2, -D2), xnu);
-    angf = f2_add(angf, atan2f(pj.im, pj.re));
+    angf = f2_add(angf, m_atan2(pj.im, pj.re));
     angf = f2_add(angf, -W * av);
     const float ang = angf.hi;
-    const float mod = exp2f(t.hi) * (1.0f + t.lo * LN2_F);
+    const float mod = m_exp2(t.hi) * (1.0f + t.lo * LN2_F);
     float sn, cs;
-    sincosf(ang, &sn, &cs);
+    m_sincos(ang, &sn, &cs);
     {
         const float c2 = fmaf(-angf.lo, sn, cs), s2 = fmaf(angf.lo, cs, sn);
         cs = c2;
@@ -1243,11 +1288,11 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     out[0] = c;
     if (FT_K > 1) {
         const float er =
-            LN2_F * ((float)(cpsi.e - FT_LOOPS * mv.e) + (log2f(cpsi.m) - (float)FT_LOOPS * log2f(mv.m)));
+            LN2_F * ((float)(cpsi.e - FT_LOOPS * mv.e) + (m_log2(cpsi.m) - (float)FT_LOOPS * m_log2(mv.m)));
         const float ei = apsi - (float)FT_LOOPS * av;
 #pragma unroll
         for (int j = 1; j < FT_K; j++) {
-            c = c * cmk(er / (float)j, ei / (float)j);
+            c = c * cmk(er * (1.0f / (float)j), ei * (1.0f / (float)j));
             out[j] = c;
         }
     }
@@ -1281,14 +1326,16 @@ static __device__ __forceinline__ void dd_add(double& ah, double& al, double bh,
 }
 
 // Block reduction of per-thread (hi, lo) accumulators into acc_out[blockIdx.x]
-static __device__ void block_reduce(double* vals /* ACC_SLOTS per thread, (hi,lo) pairs for the first 8K */,
-                                    double* acc_out)
+static __device__ __noinline__ void block_reduce(double* vals /* ACC_SLOTS per thread, (hi,lo) pairs for the first 8K */,
+                                                 double* acc_out)
 {
+    // runs once per thread at the end: kept as loops (small code), not unrolled
     __shared__ double red[FT_BLOCK / 32][ACC_SLOTS];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll 1
     for (int s = 0; s < 8 * FT_K; s += 2) {
         double h = vals[s], l = vals[s + 1];
-#pragma unroll
+#pragma unroll 1
         for (int off = 16; off; off >>= 1) {
             double oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
             dd_add(h, l, oh, ol);
@@ -1298,23 +1345,28 @@ static __device__ void block_reduce(double* vals /* ACC_SLOTS per thread, (hi,lo
             red[wid][s + 1] = l;
         }
     }
+#pragma unroll 1
     for (int s = 8 * FT_K; s < ACC_SLOTS; s++) {
         double v = vals[s];
-#pragma unroll
+#pragma unroll 1
         for (int off = 16; off; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
         if (lane == 0) red[wid][s] = v;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
         double* o = acc_out + (size_t)blockIdx.x * ACC_SLOTS;
+#pragma unroll 1
         for (int s = 0; s < 8 * FT_K; s += 2) {
             double h = red[0][s], l = red[0][s + 1];
+#pragma unroll 1
             for (int w = 1; w < FT_BLOCK / 32; w++) dd_add(h, l, red[w][s], red[w][s + 1]);
             o[s] = h;
             o[s + 1] = l;
         }
+#pragma unroll 1
         for (int s = 8 * FT_K; s < ACC_SLOTS; s++) {
             double v = 0.0;
+#pragma unroll 1
             for (int w = 0; w < FT_BLOCK / 32; w++) v += red[w][s];
             o[s] = v;
         }

@@ -197,6 +197,9 @@ struct ft_plan {
         k.minb = prec == 0 ? 1 : tuned_minb;
         if (const char* e = std::getenv("FEYNTROP_GB300_BLOCK")) k.block = std::atoi(e);
         if (const char* e = std::getenv("FEYNTROP_GB300_MINB")) k.minb = std::atoi(e);
+        // out-of-line FP32 transcendentals pay off where the code is largest (deformed)
+        k.variant = P.deformed() ? 1 : 0;
+        if (const char* e = std::getenv("FEYNTROP_GB300_VARIANT")) k.variant = std::atoi(e);
         k.ek = P.ek;
         k.el = P.el;
         // small tables are staged per block in shared memory; from E = 11 on the table is

@@ -42,7 +42,15 @@ N_SECTOR_DUMP = 32
 SEEDS = list(range(32))
 
 
-def kin_input(edges, rules, point, D, K, lam, N=1000, seed=0):
+SYMBOLIC = {}
+
+
+def kin_input(edges, rules, point, D, K, lam, N=1000, seed=0, name=None):
+    if name:
+        # the front end's own arguments, for checking a re-implementation of it
+        SYMBOLIC[name] = {"edges": [[list(e[0]), e[1], str(e[2])] for e in edges],
+                          "rules": [[int(r[0].indices[0]), int(r[0].indices[1]), str(r[1])] for r in rules],
+                          "point": [[k, v] for k, v in point], "D0": D, "eps_order": K, "Lambda": lam}
     P, m2 = ref_py.prepare_kinematic_data(edges, rules, point)
     return {
         "graph": [[list(e[0]), e[1]] for e in edges],
@@ -60,26 +68,26 @@ def suite_cases():
     """The seven inputs of the reference's tests/test_suite.py:47-117."""
     c = {}
     c["1L_2pt"] = (kin_input([((0, 1), 1, "mm0"), ((0, 1), 2, "mm1")], [(sp[0, 0], "pp")],
-                             [("mm0", 0.2), ("mm1", 1.2), ("pp", 3)], 4, 5, 1))
+                             [("mm0", 0.2), ("mm1", 1.2), ("pp", 3)], 4, 5, 1, name="1L_2pt"))
     tri = [((0, 1), 1, "mm0"), ((1, 2), 1, "mm1"), ((2, 0), 1, "mm2")]
     tri_rules = [(sp[0, 0], "pp0"), (sp[1, 1], "pp1"), (sp[0, 1], "(s01-pp0-pp1)/2")]
     c["1L_3pt_eucl"] = kin_input(tri, tri_rules, [("mm0", 0.2), ("mm1", 1.2), ("mm2", 2.2), ("pp0", -4),
-                                                  ("pp1", -5), ("s01", -13)], 4, 5, 1)
+                                                  ("pp1", -5), ("s01", -13)], 4, 5, 1, name="1L_3pt_eucl")
     c["1L_3pt_mink"] = kin_input(tri, tri_rules, [("mm0", 0.01), ("mm1", 0.5), ("mm2", 1), ("pp0", 1),
-                                                  ("pp1", 4), ("s01", 3)], 4, 5, 1)
+                                                  ("pp1", 4), ("s01", 3)], 4, 5, 1, name="1L_3pt_mink")
     c["2L_2pt_ladder"] = kin_input(
         [((0, 2), 1, "mm0"), ((0, 3), 1, "mm1"), ((1, 2), 1, "mm2"), ((1, 3), 1, "mm3"), ((2, 3), 1, "mm4")],
         [(sp[0, 0], "pp")], [("mm0", 0.1), ("mm1", 0.2), ("mm2", 0.3), ("mm3", 0.4), ("mm4", 0.5), ("pp", 3)],
-        4, 4, 0.5)
+        4, 4, 0.5, name="2L_2pt_ladder")
     c["2L_4pt_ladder"] = kin_input(
         [((0, 1), 1, "0"), ((0, 4), 1, "0"), ((1, 5), 1, "0"), ((5, 4), 1, "0"), ((5, 2), 1, "0"),
          ((4, 3), 1, "0"), ((3, 2), 1, "0")],
         [(sp[0, 0], "pp0"), (sp[1, 1], "pp1"), (sp[2, 2], "pp2"), (sp[0, 1], "(s01-pp0-pp1)/2"),
          (sp[0, 2], "(s02-pp0-pp2)/2"), (sp[1, 2], "(s12-pp1-pp2)/2")],
-        [("pp0", 1.2), ("pp1", 1.3), ("pp2", 1.4), ("s01", 2.1), ("s02", 2.2), ("s12", 2.3)], 4, 5, 1)
+        [("pp0", 1.2), ("pp1", 1.3), ("pp2", 1.4), ("s01", 2.1), ("s02", 2.2), ("s12", 2.3)], 4, 5, 1, name="2L_4pt_ladder")
     c["2L_3pt_tutorial"] = kin_input(
         [((0, 1), 1, "mm"), ((1, 3), 1, "mm"), ((3, 2), 1, "mm"), ((2, 0), 1, "mm"), ((0, 3), 1, "mm")],
-        [(sp[0, 0], "0"), (sp[1, 1], "0"), (sp[0, 1], "s01/2")], [("mm", 0.2), ("s01", 1)], 2, 5, 7.6)
+        [(sp[0, 0], "0"), (sp[1, 1], "0"), (sp[0, 1], "s01/2")], [("mm", 0.2), ("s01", 1)], 2, 5, 7.6, name="2L_3pt_tutorial")
     c["2L_5pt_box_pent"] = kin_input(
         [((0, 1), 1, "0"), ((1, 2), 1, "mm"), ((2, 6), 1, "0"), ((6, 3), 1, "mm"), ((3, 4), 1, "0"),
          ((4, 5), 1, "mm"), ((5, 0), 1, "0"), ((5, 6), 1, "mm")],
@@ -87,7 +95,7 @@ def suite_cases():
          (sp[0, 2], "(s02-mm)/2"), (sp[0, 3], "(s03-mm)/2"), (sp[1, 2], "(s12-2*mm)/2"),
          (sp[1, 3], "(s13-2*mm)/2"), (sp[2, 3], "(s23-2*mm)/2")],
         [("mm", 1 / 2), ("s01", 2.2), ("s02", 2.3), ("s02", 2.3), ("s03", 2.4), ("s12", 2.5), ("s13", 2.6),
-         ("s23", 2.7)], 6, 5, 0.28)
+         ("s23", 2.7)], 6, 5, 0.28, name="2L_5pt_box_pent")
     return c
 
 
@@ -199,7 +207,7 @@ def main():
     cases = suite_cases()
     cases.update(extra_cases())
     pins = {"generator": "tests/golden/make_golden.py", "N_aggregate": N_AGG, "seeds": SEEDS, "cases": {},
-            "suite_expectations": suite_expectations()}
+            "suite_expectations": suite_expectations(), "suite_symbolic": SYMBOLIC}
     for name, inp in cases.items():
         print("case", name, flush=True)
         table = run_harness(inp, ["table"])
