@@ -54,6 +54,19 @@ def algorithmic_flops(E, V, K, deformed):
     return f
 
 
+def dram_traffic(key):
+    """DRAM bytes (read + write) per launch of a kernel from the committed ncu summary
+    profiles/dram_traffic.txt (lines: kernel, precision, workload, bytes per launch)."""
+    path = os.path.join(HERE, "profiles", "dram_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 4 and not line.startswith("#") and " ".join(parts[:3]) == key:
+            return float(parts[3])
+    return None
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
 
@@ -308,10 +321,7 @@ def main():
         v, nsample, kind = cpu_rate(inp, args.cpu_seconds, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": "%d samples of the double-box workload (same stream), all host threads" % nsample}
-    prof = os.path.join(HERE, "profiles", "traffic.json")
-    traffic = None
-    if os.path.exists(prof):
-        traffic = json.load(open(prof)).get("ft_sample_mixed_double_box_bytes_per_launch")
+    traffic = dram_traffic("ft_sample mixed double_box")
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
