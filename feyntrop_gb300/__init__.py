@@ -34,7 +34,9 @@ MIXED = 1
 
 EXPORTED = ["ft_plan_create", "ft_plan_destroy", "ft_plan_get_info", "ft_plan_log_line", "ft_integrate",
             "ft_integrate_batch", "ft_finalize_moments", "ft_sample_records", "ft_run_json", "ft_free",
-            "ft_precompile", "ft_last_error", "ft_version", "ft_subgraph_table", "ft_device_peaks", "ft_integrate_noalloc"]
+            "ft_precompile", "ft_last_error", "ft_version", "ft_subgraph_table", "ft_device_peaks", "ft_integrate_noalloc",
+            "ft_batch_create", "ft_batch_destroy", "ft_batch_run", "ft_batch_get_info"]
+PRECOMPILE_BATCH = 0x100
 
 
 class FeyntropError(RuntimeError):
@@ -76,6 +78,13 @@ class Result(ctypes.Structure):
                 ("seconds_sampling", ctypes.c_double), ("kernel_launches", ctypes.c_int32)]
 
 
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("num_integrals", ctypes.c_int32), ("num_classes", ctypes.c_int32),
+                ("graph_captures", ctypes.c_int32), ("kernel_launches", ctypes.c_int32),
+                ("work_items", ctypes.c_uint64), ("fp64_queue_capacity", ctypes.c_uint64),
+                ("kernel_ms", ctypes.c_double)]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -107,6 +116,11 @@ def lib():
             L.ft_precompile.argtypes = [ctypes.POINTER(Problem), ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
             L.ft_integrate_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(RunOptions), ctypes.c_void_p]
             L.ft_device_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+            L.ft_batch_create.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.POINTER(ctypes.c_void_p)]
+            L.ft_batch_destroy.argtypes = [ctypes.c_void_p]
+            L.ft_batch_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+            L.ft_batch_get_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(BatchInfo)]
             L.ft_subgraph_table.argtypes = [ctypes.POINTER(Problem)] + [ctypes.c_void_p] * 4 + [
                 ctypes.POINTER(PlanInfo)]
             _lib = L
@@ -219,6 +233,97 @@ class Plan:
         opts = RunOptions(int(count), int(seed), int(first_sample), int(precision), None)
         _check(lib().ft_sample_records(self.h, ctypes.byref(opts), _ptr(order), _ptr(X), _ptr(R), _ptr(flags)))
         return {"order": order.astype(np.int32), "X": X, "R": R[..., 0] + 1j * R[..., 1], "flags": flags}
+
+
+class _ResultArrays:
+    """Caller-owned result buffers of one integral."""
+
+    def __init__(self, K):
+        self.K = K
+        self.arr = np.zeros((4, K))
+        self.mom = (Moments * (2 * K))()
+        self.res = Result(K, _ptr(self.arr[0]).value, _ptr(self.arr[1]).value, _ptr(self.arr[2]).value,
+                          _ptr(self.arr[3]).value, ctypes.cast(self.mom, ctypes.c_void_p).value)
+
+    def as_dict(self, IGtr):
+        arr, res, K = self.arr, self.res, self.K
+        return {
+            "integral": [[[arr[0, j], arr[1, j]], [arr[2, j], arr[3, j]]] for j in range(K)],
+            "IGtr": IGtr,
+            "moments": [[m.n, m.s1_hi, m.s1_lo, m.s2_hi, m.s2_lo] for m in self.mom],
+            "kept": res.kept, "dropped": res.dropped, "fp64_fallback": res.fp64_fallback,
+            "exact_steps": res.exact_steps, "robust": res.robust, "kernel_ms": res.kernel_ms,
+            "seconds_sampling": res.seconds_sampling, "kernel_launches": res.kernel_launches,
+        }
+
+
+class Batch:
+    """Many integrals in one CUDA graph launch (ft_batch_*): one persistent sampling
+    launch per kernel class (topology, eps orders, regime), classes side by side.
+    The plans must stay open while the batch is used."""
+
+    def __init__(self, plans, precision=MIXED):
+        self.plans = list(plans)
+        arr = (ctypes.c_void_p * len(self.plans))(*[p.h.value for p in self.plans])
+        h = ctypes.c_void_p()
+        _check(lib().ft_batch_create(ctypes.cast(arr, ctypes.c_void_p), len(self.plans), int(precision),
+                                     ctypes.byref(h)))
+        self.h = h
+        self.precision = precision
+
+    def run(self, N, seeds=0, first_samples=0, stream=None):
+        """N, seeds, first_samples: scalars or one per integral; returns one result
+        dict per integral (as Plan.integrate)."""
+        n = len(self.plans)
+        Ns = list(N) if hasattr(N, "__len__") else [N] * n
+        ss = list(seeds) if hasattr(seeds, "__len__") else [seeds] * n
+        fs = list(first_samples) if hasattr(first_samples, "__len__") else [first_samples] * n
+        opts = (RunOptions * n)(*[RunOptions(int(Ns[i]), int(ss[i]), int(fs[i]), int(self.precision),
+                                             stream if i == 0 else None) for i in range(n)])
+        ras = [_ResultArrays(p.K) for p in self.plans]
+        res = (Result * n)(*[r.res for r in ras])
+        _check(lib().ft_batch_run(self.h, ctypes.cast(opts, ctypes.c_void_p), ctypes.cast(res, ctypes.c_void_p)))
+        out = []
+        for i, r in enumerate(ras):
+            r.res = res[i]
+            out.append(r.as_dict(self.plans[i].info["IGtr"]))
+        return out
+
+    def info(self):
+        bi = BatchInfo()
+        _check(lib().ft_batch_get_info(self.h, ctypes.byref(bi)))
+        return {f: getattr(bi, f) for f, _ in BatchInfo._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().ft_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def integrate_batch(plans, N, seeds=0, precision=MIXED, first_samples=0):
+    """ft_integrate_batch: a transient batch over the plans (same precision for all)."""
+    n = len(plans)
+    Ns = list(N) if hasattr(N, "__len__") else [N] * n
+    ss = list(seeds) if hasattr(seeds, "__len__") else [seeds] * n
+    fs = list(first_samples) if hasattr(first_samples, "__len__") else [first_samples] * n
+    arr = (ctypes.c_void_p * n)(*[p.h.value for p in plans])
+    opts = (RunOptions * n)(*[RunOptions(int(Ns[i]), int(ss[i]), int(fs[i]), int(precision), None)
+                               for i in range(n)])
+    ras = [_ResultArrays(p.K) for p in plans]
+    res = (Result * n)(*[r.res for r in ras])
+    _check(lib().ft_integrate_batch(ctypes.cast(arr, ctypes.c_void_p), n, ctypes.cast(opts, ctypes.c_void_p),
+                                    ctypes.cast(res, ctypes.c_void_p)))
+    out = []
+    for i, r in enumerate(ras):
+        r.res = res[i]
+        out.append(r.as_dict(plans[i].info["IGtr"]))
+    return out
 
 
 def finalize_moments(moments, K, real_only):

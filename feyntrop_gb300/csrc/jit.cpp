@@ -40,6 +40,7 @@ std::string kernel_source(const kernel_key& k)
     s << "#define FT_ONLY_PSI " << k.only_psi << "\n#define FT_RECORD " << k.record << "\n";
     s << "#define FT_BLOCK " << k.block << "\n#define FT_TABLE_GLOBAL " << k.table_global << "\n";
     s << "#define FT_MINB " << k.minb << "\n#define FT_VARIANT " << k.variant << "\n";
+    s << "#define FT_BATCH " << k.batch << "\n";
     s << "__device__ constexpr int FT_EK[" << k.E << "] = {";
     for (int e = 0; e < k.E; e++) s << (e ? "," : "") << k.ek[e];
     s << "};\n__device__ constexpr int FT_EL[" << k.E << "] = {";
@@ -186,7 +187,8 @@ static std::string key_string(const kernel_key& k)
 {
     std::ostringstream s;
     s << k.E << "," << k.V << "," << k.K << "," << k.loops << "," << k.rank << "," << k.prec << "," << k.mode << ","
-      << k.only_psi << "," << k.record << "," << k.block << "," << k.table_global << "," << k.minb << "," << k.variant;
+      << k.only_psi << "," << k.record << "," << k.block << "," << k.table_global << "," << k.minb << "," << k.variant
+      << "," << k.batch;
     for (int e = 0; e < k.E; e++) s << ";" << k.ek[e] << "-" << k.el[e];
     return s.str();
 }
@@ -219,8 +221,10 @@ const kernel_set& get_kernels(const kernel_key& key)
     ks.block = key.block;
     const std::string cubin = cubin_for(key, &ks.compile_seconds);
     check(drv().ModuleLoadData(&ks.module, cubin.data()), "cuModuleLoadData");
-    check(drv().ModuleGetFunction(&ks.sample, ks.module, "ft_sample"), "cuModuleGetFunction(ft_sample)");
-    if (key.prec == 0) check(drv().ModuleGetFunction(&ks.queue, ks.module, "ft_sample_queue"), "cuModuleGetFunction(queue)");
+    const char* sname = key.batch ? "ft_sample_batch" : "ft_sample";
+    const char* qname = key.batch ? "ft_sample_queue_batch" : "ft_sample_queue";
+    check(drv().ModuleGetFunction(&ks.sample, ks.module, sname), "cuModuleGetFunction(sampling kernel)");
+    if (key.prec == 0) check(drv().ModuleGetFunction(&ks.queue, ks.module, qname), "cuModuleGetFunction(queue)");
     ks.smem = table_smem_bytes(key);
     CUfunction fs[2] = {ks.sample, ks.queue};
     for (CUfunction f : fs) {

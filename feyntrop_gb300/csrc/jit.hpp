@@ -24,13 +24,14 @@ struct kernel_key {
     int block = 128;
     int minb = 1;           // minimum resident blocks per SM asked of the register allocator
     int variant = 0;        // code-size options of the kernel body (FT_VARIANT)
+    int batch = 0;          // 1: the batch kernels (many integrals of the topology per launch)
     std::vector<int> ek, el;
 };
 
 struct kernel_set {
     CUmodule module = nullptr;
-    CUfunction sample = nullptr;   // ft_sample
-    CUfunction queue = nullptr;    // ft_sample_queue (FP64 modules only)
+    CUfunction sample = nullptr;   // ft_sample (ft_sample_batch in batch modules)
+    CUfunction queue = nullptr;    // ft_sample_queue / ft_sample_queue_batch (FP64 modules only)
     int block = 128;
     unsigned smem = 0;             // dynamic shared memory per block
     int regs = 0;

@@ -7,6 +7,9 @@
 //  ft_finalize_parts   sums the per-block partial moments of one integration into a
 //                      single vector: double-double for the moment slots, plain for
 //                      the counters.
+//  ft_batch_item_states  stream states of the work items of a batch (one warp per
+//                      integral, GF(2) skip-ahead).
+//  ft_batch_finalize   per-integral sums of a batch's work items and FP64 pass.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -98,6 +101,105 @@ __global__ void ft_finalize_parts(const double* __restrict__ parts, int nparts, 
         double v = 0.0;
         for (int p = 0; p < nparts; p++) v += parts[(size_t)p * slots + s];
         out[s] = v;
+    }
+}
+
+// ------------------------------------------------------------------ batches
+// Device views of the batch descriptors (layouts shared with the batch kernels of the
+// sampling module and with batch.cpp).
+struct batch_inst_view {
+    const void* prm;
+    const void* tab;
+    u64 nsamples, first_item, nitems, pad[3];
+};
+struct item_prep {
+    u64 s[4];         // seed state of the instance's stream
+    u64 skip;         // draws before its first sample
+    u64 first_item, nitems, pad;
+};
+
+__device__ __forceinline__ u64 word_of(const u64 (&g)[4], int w)
+{
+    return w == 0 ? g[0] : w == 1 ? g[1] : w == 2 ? g[2] : g[3];
+}
+
+// g <- M g over GF(2) by one warp: lane l owns input bits 8l .. 8l+7 (column c of M is
+// the four words M[4c .. 4c+3]); the partial results are XOR-reduced across the warp
+__device__ __forceinline__ void warp_gf2_apply(const u64* __restrict__ M, u64 (&g)[4], int lane)
+{
+    u64 r0 = 0, r1 = 0, r2 = 0, r3 = 0;
+    const u64 sw = word_of(g, lane >> 3);
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const int c = lane * 8 + k;
+        const u64 mask = 0ull - ((sw >> (((lane & 7) << 3) + k)) & 1ull);
+        const ulonglong2 lo = __ldg((const ulonglong2*)(M + 4 * c)), hi = __ldg((const ulonglong2*)(M + 4 * c + 2));
+        r0 ^= lo.x & mask;
+        r1 ^= lo.y & mask;
+        r2 ^= hi.x & mask;
+        r3 ^= hi.y & mask;
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+        r0 ^= __shfl_xor_sync(0xffffffffu, r0, off);
+        r1 ^= __shfl_xor_sync(0xffffffffu, r1, off);
+        r2 ^= __shfl_xor_sync(0xffffffffu, r2, off);
+        r3 ^= __shfl_xor_sync(0xffffffffu, r3, off);
+    }
+    g[0] = r0;
+    g[1] = r1;
+    g[2] = r2;
+    g[3] = r3;
+}
+
+// one warp per instance: the stream state of each of its work items' first samples
+__global__ void __launch_bounds__(128) ft_batch_item_states(const item_prep* __restrict__ d, int n,
+                                                            const u64* __restrict__ tpow,
+                                                            const u64* __restrict__ itemM, u64* __restrict__ out)
+{
+    const int w = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5), lane = (int)(threadIdx.x & 31u);
+    if (w >= n) return;   // the whole warp
+    u64 g[4] = {d[w].s[0], d[w].s[1], d[w].s[2], d[w].s[3]};
+    const u64 skip = d[w].skip;
+    for (int b = 0; b < 64; b++)
+        if ((skip >> b) & 1ull) warp_gf2_apply(tpow + (size_t)b * 1024, g, lane);
+    const u64 f = d[w].first_item, m = d[w].nitems;
+    for (u64 k = 0; k < m; k++) {
+        if (lane < 4) out[(f + k) * 4 + lane] = word_of(g, lane);
+        if (k + 1 < m) warp_gf2_apply(itemM, g, lane);
+    }
+}
+
+// Per instance: the sums of its work items (double-double for the moment pairs) plus
+// the FP64 pass's sums (qacc, NULL for FP64 batches).  One thread per (instance,
+// moment pair or counter).  Slots: 8K moments as 4K (hi, lo) pairs, then kept,
+// dropped, queued, exact, robust, 3 spare; qacc: 4K sums, kept, dropped, robust, spare.
+__global__ void ft_batch_finalize(const batch_inst_view* __restrict__ inst, int n, const double* __restrict__ parts,
+                                  int K, const double* __restrict__ qacc, double* __restrict__ out)
+{
+    const int slots = 8 * K + 8, units = 4 * K + 8, qslots = 4 * K + 4;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)n * units) return;
+    const int m = (int)(t / units), u = (int)(t % units);
+    const u64 f = inst[m].first_item, cnt = inst[m].nitems;
+    double* o = out + (size_t)m * slots;
+    if (u < 4 * K) {
+        double h = 0.0, l = 0.0;
+        for (u64 k = 0; k < cnt; k++)
+            dd_add(h, l, parts[(f + k) * slots + 2 * u], parts[(f + k) * slots + 2 * u + 1]);
+        if (qacc) dd_add(h, l, qacc[(size_t)m * qslots + u], 0.0);
+        o[2 * u] = h;
+        o[2 * u + 1] = l;
+    } else {
+        const int c = u - 4 * K;
+        double v = 0.0;
+        for (u64 k = 0; k < cnt; k++) v += parts[(f + k) * slots + 8 * K + c];
+        if (qacc) {
+            if (c == 0) v += qacc[(size_t)m * qslots + 4 * K];
+            if (c == 1) v += qacc[(size_t)m * qslots + 4 * K + 1];
+            if (c == 4) v += qacc[(size_t)m * qslots + 4 * K + 2];
+        }
+        o[8 * K + c] = v;
     }
 }
 
@@ -199,6 +301,24 @@ cudaError_t noalloc_scratch(noalloc_layout* out)
 cudaError_t launch_lane_powers(const u64* tpow, u64 S, int nbits, u64* out, cudaStream_t st)
 {
     ft_gf2_lane_powers<<<1, 256, 0, st>>>(tpow, S, nbits, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_item_states(const void* prep, int n, const u64* tpow, const u64* itemM, u64* out,
+                                     cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    ft_batch_item_states<<<(n + 3) / 4, 128, 0, st>>>((const item_prep*)prep, n, tpow, itemM, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_finalize(const void* inst, int n, const double* parts, int K, const double* qacc,
+                                  double* out, cudaStream_t st)
+{
+    if (n <= 0) return cudaSuccess;
+    const long long threads = (long long)n * (4 * K + 8);
+    ft_batch_finalize<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>((const batch_inst_view*)inst, n, parts, K,
+                                                                         qacc, out);
     return cudaGetLastError();
 }
 

@@ -9,6 +9,14 @@ namespace ft {
 cudaError_t launch_lane_powers(const unsigned long long* tpow, unsigned long long S, int nbits,
                                unsigned long long* out, cudaStream_t st);
 
+// Batches (layouts in aot.cu): item stream states from per-instance item_prep records
+// (one warp per instance), and the per-instance sums of the work items plus the FP64
+// pass (qacc may be NULL).
+cudaError_t launch_batch_item_states(const void* prep, int n, const unsigned long long* tpow,
+                                     const unsigned long long* itemM, unsigned long long* out, cudaStream_t st);
+cudaError_t launch_batch_finalize(const void* inst, int n, const double* parts, int K, const double* qacc,
+                                  double* out, cudaStream_t st);
+
 // out[s] = sum over parts of parts[p * slots + s]; slots [0, ndd) are (hi, lo) pairs
 cudaError_t launch_finalize(const double* parts, int nparts, int slots, int ndd, double* out, cudaStream_t st);
 

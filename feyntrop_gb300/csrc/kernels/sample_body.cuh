@@ -46,6 +46,10 @@
 #ifndef FT_MINB
 #define FT_MINB 1
 #endif
+// 1: the module holds the batch kernels (many integrals of this topology per launch)
+#ifndef FT_BATCH
+#define FT_BATCH 0
+#endif
 
 typedef unsigned long long u64;
 typedef unsigned int u32;
@@ -1325,9 +1329,9 @@ static __device__ __forceinline__ void dd_add(double& ah, double& al, double bh,
     al = err - (ah - s);
 }
 
-// Block reduction of per-thread (hi, lo) accumulators into acc_out[blockIdx.x]
+// Block reduction of per-thread (hi, lo) accumulators into o[0 .. ACC_SLOTS)
 static __device__ __noinline__ void block_reduce(double* vals /* ACC_SLOTS per thread, (hi,lo) pairs for the first 8K */,
-                                                 double* acc_out)
+                                                 double* o)
 {
     // runs once per thread at the end: kept as loops (small code), not unrolled
     __shared__ double red[FT_BLOCK / 32][ACC_SLOTS];
@@ -1354,7 +1358,6 @@ static __device__ __noinline__ void block_reduce(double* vals /* ACC_SLOTS per t
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double* o = acc_out + (size_t)blockIdx.x * ACC_SLOTS;
 #pragma unroll 1
         for (int s = 0; s < 8 * FT_K; s += 2) {
             double h = red[0][s], l = red[0][s + 1];
@@ -1578,7 +1581,8 @@ struct accum {
     }
 #endif
 
-    __device__ __forceinline__ void finish(double* acc_out)
+    // block-wide: every thread of the block calls it; the block's sums go to dst[0 .. ACC_SLOTS)
+    __device__ __forceinline__ void finish(double* dst)
     {
 #if FT_PREC == 1
         fold();
@@ -1602,7 +1606,7 @@ struct accum {
         vals[ACC_ROBUST] = robust;
 #pragma unroll
         for (int s = ACC_ROBUST + 1; s < ACC_SLOTS; s++) vals[s] = 0.0;
-        block_reduce(vals, acc_out);
+        block_reduce(vals, dst);
     }
 };
 
@@ -1650,40 +1654,23 @@ static __device__ __forceinline__ void sample64(xo& g, const table_ref& tr, cons
 }
 #endif
 
-// ------------------------------------------------------------------ main kernel
-// Thread t of the launch owns samples [t*chunk, min(nsamples, (t+1)*chunk)) counted
-// from the launch's first sample, whose stream state is (s0..s3).  Block b writes
-// its partial sums to acc_out[b * ACC_SLOTS ...].  In the mixed form, samples whose
-// FP32 evaluation is not trustworthy are appended to `queue` (index and stream
-// state, 5 words) for the FP64 pass and left out of the sums here.
-extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
-    const double* __restrict__ prm, const unsigned char* __restrict__ tab, const u64* __restrict__ lanepw,
-    int lanebits, u64 s0, u64 s1, u64 s2, u64 s3, u64 nsamples, u64 chunk, double* __restrict__ acc_out,
-    u64* __restrict__ queue, unsigned int* __restrict__ qcount, unsigned int qcap,
-    unsigned char* __restrict__ rec_order, double* __restrict__ rec_X, double* __restrict__ rec_R,
-    unsigned char* __restrict__ rec_flags)
+// ------------------------------------------------------------------ one thread's samples
+// Samples [first, last) of the stream, g holding the state of sample `first`.  In the
+// mixed form, samples whose FP32 evaluation is not trustworthy are queued for the FP64
+// pass and left out of the sums here: 5 words (sample index, stream state) in the
+// single-integral kernels, one word `qtag | (i - first)` in the batch kernels (the
+// FP64 pass re-derives the state from the work item).
+static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, const double* __restrict__ prm,
+                                                    u64 first, u64 last, accum& A, u64* __restrict__ queue,
+                                                    unsigned int* __restrict__ qcount, unsigned int qcap, u64 qtag,
+                                                    unsigned char* __restrict__ rec_order, double* __restrict__ rec_X,
+                                                    double* __restrict__ rec_R, unsigned char* __restrict__ rec_flags)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
-    const table_ref tr = stage_table(smem, tab);
-
-    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;
 #if FT_PREC == 1
     const float* pf = (const float*)(prm + P_SIZE);
     const float* pd = (const float*)(prm + P_SIZE + (P_SIZE + 1) / 2);   // two-float pairs
 #endif
-    xo g;
-    g.a = s0;
-    g.b = s1;
-    g.c = s2;
-    g.d = s3;
-    skip_lanes(g, t, lanepw, lanebits);
-
-    u64 first = (u64)t * chunk;
-    u64 last = first + chunk;
-    if (last > nsamples) last = nsamples;
-
-    accum A;
-    A.init(smem + ACC_SMEM_OFFSET);
+    (void)qtag;
     for (u64 i = first; i < last; i++) {
 #if FT_PREC == 0
         sample64(g, tr, prm, i, A, 0, rec_order, rec_X, rec_R, rec_flags);
@@ -1706,12 +1693,16 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
             A.note32(0.0f, 1.0f, (float)ex);
             const unsigned int slot = atomicAdd(qcount, 1u);
             if (slot < qcap) {
+#if FT_BATCH
+                queue[slot] = qtag | (i - first);
+#else
                 u64* q = queue + (size_t)slot * 5;
                 q[0] = i;
                 q[1] = g0.a;
                 q[2] = g0.b;
                 q[3] = g0.c;
                 q[4] = g0.d;
+#endif
             }
             if (FT_RECORD) write_record(i, ord, R, false, flags, rec_order, rec_R, rec_flags);
             continue;
@@ -1726,7 +1717,39 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
         if (FT_RECORD) write_record(i, ord, R, ok, flags, rec_order, rec_R, rec_flags);
 #endif
     }
-    A.finish(acc_out);
+}
+
+#if !FT_BATCH
+// ------------------------------------------------------------------ single-integral kernels
+// Thread t of the launch owns samples [t*chunk, min(nsamples, (t+1)*chunk)) counted
+// from the launch's first sample, whose stream state is (s0..s3).  Block b writes
+// its partial sums to acc_out[b * ACC_SLOTS ...].
+extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
+    const double* __restrict__ prm, const unsigned char* __restrict__ tab, const u64* __restrict__ lanepw,
+    int lanebits, u64 s0, u64 s1, u64 s2, u64 s3, u64 nsamples, u64 chunk, double* __restrict__ acc_out,
+    u64* __restrict__ queue, unsigned int* __restrict__ qcount, unsigned int qcap,
+    unsigned char* __restrict__ rec_order, double* __restrict__ rec_X, double* __restrict__ rec_R,
+    unsigned char* __restrict__ rec_flags)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    const table_ref tr = stage_table(smem, tab);
+
+    const u32 t = blockIdx.x * blockDim.x + threadIdx.x;
+    xo g;
+    g.a = s0;
+    g.b = s1;
+    g.c = s2;
+    g.d = s3;
+    skip_lanes(g, t, lanepw, lanebits);
+
+    u64 first = (u64)t * chunk;
+    u64 last = first + chunk;
+    if (last > nsamples) last = nsamples;
+
+    accum A;
+    A.init(smem + ACC_SMEM_OFFSET);
+    sample_range(g, tr, prm, first, last, A, queue, qcount, qcap, 0, rec_order, rec_X, rec_R, rec_flags);
+    A.finish(acc_out + (size_t)blockIdx.x * ACC_SLOTS);
 }
 
 #if FT_PREC == 0
@@ -1752,7 +1775,169 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue(
         g.d = q[4];
         sample64(g, tr, prm, q[0], A, REC_QUEUED, rec_order, rec_X, rec_R, rec_flags);
     }
-    A.finish(acc_out);
+    A.finish(acc_out + (size_t)blockIdx.x * ACC_SLOTS);
 }
 #endif
+
+#else
+// ------------------------------------------------------------------ batch kernels
+// Many integrals of this topology (each with its own kinematics, table, seed and N)
+// in one persistent launch.  The samples of instance i are cut into work items of
+// FT_BLOCK * chunk consecutive samples; items are numbered instance after instance
+// (instance i owns items [first_item, first_item + nitems)).  A block takes the next
+// item from a device counter, thread t of the block owns samples
+// [item_base + t*chunk, item_base + (t+1)*chunk) of the instance, and the block writes
+// the item's sums to acc_out[item * ACC_SLOTS ...].  item_state[item] is the stream
+// state of the item's first sample (computed by a preparation kernel); thread t
+// reaches its own first sample with the lane skip matrices (T^(chunk * (2E-1)))^(2^b).
+struct batch_inst {
+    const double* prm;          // parameter block of the instance (P_SIZE doubles, floats, two-floats)
+    const unsigned char* tab;   // J(gamma) table of the instance (global layout)
+    u64 nsamples;
+    u64 first_item;
+    u64 nitems;
+    u64 pad[3];
+};
+
+// FP64-pass queue word: item << 28 | lane << 18 | offset of the sample in the lane's chunk
+#define BQ_ITEM_SHIFT 28
+#define BQ_LANE_SHIFT 18
+#define BQ_OFF_MASK ((1ull << BQ_LANE_SHIFT) - 1ull)
+#define BQ_LANE_MASK 1023ull
+
+// the instance owning `item`: the last instance whose first_item <= item
+static __device__ __forceinline__ int find_instance(const batch_inst* __restrict__ inst, int ninst, u64 item)
+{
+    int lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (inst[mid].first_item <= item)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+static __device__ __forceinline__ xo load_state(const u64* __restrict__ s)
+{
+    const ulonglong2 a = *(const ulonglong2*)s, b = *(const ulonglong2*)(s + 2);
+    xo g;
+    g.a = a.x;
+    g.b = a.y;
+    g.c = b.x;
+    g.d = b.y;
+    return g;
+}
+
+extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample_batch(
+    const batch_inst* __restrict__ inst, int ninst, const u64* __restrict__ total_items,
+    const u64* __restrict__ item_state, const u64* __restrict__ lanepw, int lanebits, u64 chunk,
+    unsigned long long* __restrict__ counter, double* __restrict__ acc_out, u64* __restrict__ queue,
+    unsigned int* __restrict__ qcount, unsigned int qcap)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ u64 s_item;
+    __shared__ int s_inst;
+    const u64 total = *total_items;
+    int cur = -1;
+    table_ref tr;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const u64 it = atomicAdd(counter, 1ull);
+            s_item = it;
+            s_inst = it < total ? find_instance(inst, ninst, it) : -1;
+        }
+        // also orders this item's table staging after every thread's previous item
+        __syncthreads();
+        const u64 it = s_item;
+        const int id = s_inst;
+        if (id < 0) break;
+        if (id != cur) {
+            tr = stage_table(smem, inst[id].tab);
+            cur = id;
+        }
+        const double* prm = inst[id].prm;
+        const u64 n = inst[id].nsamples;
+        const u64 first = (it - inst[id].first_item) * (u64)FT_BLOCK * chunk + (u64)threadIdx.x * chunk;
+        u64 last = first + chunk;
+        if (last > n) last = n;
+        xo g = load_state(item_state + it * 4);
+        skip_lanes(g, threadIdx.x, lanepw, lanebits);
+        accum A;
+        A.init(smem + ACC_SMEM_OFFSET);
+        sample_range(g, tr, prm, first, last, A, queue, qcount, qcap,
+                     (it << BQ_ITEM_SHIFT) | ((u64)threadIdx.x << BQ_LANE_SHIFT), nullptr, nullptr, nullptr, nullptr);
+        A.finish(acc_out + it * ACC_SLOTS);
+    }
+}
+
+#if FT_PREC == 0
+// FP64 pass over the samples a mixed batch launch queued.  Each entry names its work
+// item, lane and offset; the stream state is re-derived (item state, the mixed
+// launch's lane skip, offset * (2E-1) steps).  Sums go to the instance's slots of
+// qacc with atomics: per eps order j [4j + 0..3] = re f, re f^2, im f, im f^2, then
+// [4K] kept, [4K+1] dropped, [4K+2] robust.
+#define QACC_SLOTS (4 * FT_K + 4)
+extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue_batch(
+    const batch_inst* __restrict__ inst, int ninst, const u64* __restrict__ item_state,
+    const u64* __restrict__ lanepw, int lanebits, const u64* __restrict__ queue,
+    const unsigned int* __restrict__ qcount, unsigned int qcap, double* __restrict__ qacc)
+{
+    unsigned int n = *qcount;
+    if (n > qcap) n = qcap;
+    const unsigned int lane = threadIdx.x & 31u;
+    const unsigned int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) - lane;
+    const unsigned int stride = gridDim.x * blockDim.x;
+    // warp-uniform trip count: skip_lanes needs the whole warp
+    for (unsigned int k0 = warp0; k0 < n; k0 += stride) {
+        const unsigned int k = k0 + lane;
+        const bool active = k < n;
+        const u64 w = active ? queue[k] : 0ull;
+        const u64 item = w >> BQ_ITEM_SHIFT;
+        const u32 ln = active ? (u32)((w >> BQ_LANE_SHIFT) & BQ_LANE_MASK) : 0u;
+        const u64 off = w & BQ_OFF_MASK;
+        xo g = load_state(item_state + item * 4);
+        skip_lanes(g, ln, lanepw, lanebits);
+        if (!active) continue;
+        for (u64 s = 0; s < off * (2 * FT_E - 1); s++) g.next();
+        const int id = find_instance(inst, ninst, item);
+        const double* prm = inst[id].prm;
+        const unsigned char* tab = inst[id].tab;
+        table_ref tr;
+        tr.w = tab + T_W64;
+        tr.Jr = tab + T_JR64;
+        tr.ri = tab + T_RI64;
+        tr.meta = tab + T_META;
+        tr.gm = tab;
+        cx<double> R[FT_K];
+#pragma unroll
+        for (int j = 0; j < FT_K; j++) R[j] = cmk(0.0, 0.0);
+        double X[FT_E];
+        double F, Gv;
+        unsigned char ord[FT_E];
+        draw_sector64(g, tr, prm[P_JRFULL], X, F, Gv, ord);
+        bool rob = false;
+        const bool ok = integrand64(prm, X, F, Gv * F, R, rob);
+        double* q = qacc + (size_t)id * QACC_SLOTS;
+        if (rob) atomicAdd(q + 4 * FT_K + 2, 1.0);
+        if (!ok) {
+            atomicAdd(q + 4 * FT_K + 1, 1.0);
+            continue;
+        }
+        atomicAdd(q + 4 * FT_K, 1.0);
+#pragma unroll
+        for (int j = 0; j < FT_K; j++) {
+            if (FT_ONLY_PSI && j > 0) break;
+            atomicAdd(q + 4 * j + 0, R[j].re);
+            atomicAdd(q + 4 * j + 1, R[j].re * R[j].re);
+            if (ACC_PARTS == 4) {
+                atomicAdd(q + 4 * j + 2, R[j].im);
+                atomicAdd(q + 4 * j + 3, R[j].im * R[j].im);
+            }
+        }
+    }
+}
+#endif
+#endif  // FT_BATCH
 #endif  // FT_HOST_SIM

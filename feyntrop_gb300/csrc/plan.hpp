@@ -1,0 +1,122 @@
+// Internal to the library: plans, device state and error plumbing shared by the
+// single-integral path (runtime.cpp) and the batch path (batch.cpp).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <exception>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/feyntrop_gb300.h"
+#include "jit.hpp"
+#include "problem.hpp"
+#include "xoshiro.hpp"
+
+namespace ftrt {
+
+extern thread_local std::string g_error;
+
+struct cuda_error : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+inline void cu(cudaError_t e, const char* what)
+{
+    if (e != cudaSuccess) throw cuda_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// status code of the exception in flight (sets g_error)
+int status_of(const std::exception_ptr& ep);
+
+// throws std::logic_error when there is no CUDA device
+void require_device();
+
+// per-device constants: the 64 skip matrices T^(2^b), the SM count
+struct device_state {
+    unsigned long long* tpow = nullptr;
+    int sms = 0;
+};
+device_state& dev_state();
+
+// the device parameter block of a plan: the FP64 values, then the same as floats,
+// then as two-float (hi, lo) pairs (the layout the kernel body reads)
+std::vector<double> param_block(const std::vector<double>& prm);
+
+// sums of one integration (8K+8 slots) into the caller's result
+void fill_result(const ft::prepared& P, const std::vector<double>& acc, ft_result* r);
+
+}  // namespace ftrt
+
+struct ft_plan {
+    ft::prepared P;
+    std::vector<double> sigma, q, prm;
+    std::vector<unsigned char> tab;
+    int device = 0;
+    double* d_prm = nullptr;
+    unsigned char* d_tab = nullptr;
+    // scratch reused by launches
+    double* d_parts = nullptr;
+    size_t parts_cap = 0;
+    double* d_final = nullptr;
+    double* h_final = nullptr;
+    unsigned long long* d_queue = nullptr;
+    unsigned int* d_qcount = nullptr;
+    size_t qcap = 0;
+    unsigned long long* d_lanepw = nullptr;
+    unsigned long long lanepw_S = 0;
+    int lanepw_bits = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::mutex mu;
+    // launch shape of the sampling kernels (threads per block, minimum resident blocks
+    // per SM given to the register allocator), from a sweep on GB300: the mixed form
+    // gains ~1.6x on deformed integrals from 256 x 2 (168 registers instead of 255)
+    int tuned_block = 256, tuned_minb = 2;
+
+    ft::kernel_key key(int prec, int record) const
+    {
+        ft::kernel_key k;
+        k.E = P.E;
+        k.V = P.V;
+        k.K = P.K;
+        k.loops = P.loops;
+        k.rank = (int)sigma.size();
+        k.prec = prec;
+        k.mode = P.deformed() ? 1 : 0;
+        k.only_psi = P.only_psi() ? 1 : 0;
+        k.record = record;
+        k.block = tuned_block;
+        k.minb = prec == 0 ? 1 : tuned_minb;
+        if (const char* e = std::getenv("FEYNTROP_GB300_BLOCK")) k.block = std::atoi(e);
+        if (const char* e = std::getenv("FEYNTROP_GB300_MINB")) k.minb = std::atoi(e);
+        // out-of-line FP32 transcendentals pay off where the code is largest (deformed)
+        k.variant = P.deformed() ? 1 : 0;
+        if (const char* e = std::getenv("FEYNTROP_GB300_VARIANT")) k.variant = std::atoi(e);
+        k.ek = P.ek;
+        k.el = P.el;
+        // small tables are staged per block in shared memory; from E = 11 on the table is
+        // read through L1 (one cached copy per SM instead of one per block)
+        k.table_global = P.E >= 11 ? 1 : 0;
+        return k;
+    }
+
+    int slots() const { return 8 * P.K + 8; }
+
+    ~ft_plan()
+    {
+        if (d_prm) cudaFree(d_prm);
+        if (d_tab) cudaFree(d_tab);
+        if (d_parts) cudaFree(d_parts);
+        if (d_final) cudaFree(d_final);
+        if (h_final) cudaFreeHost(h_final);
+        if (d_queue) cudaFree(d_queue);
+        if (d_qcount) cudaFree(d_qcount);
+        if (d_lanepw) cudaFree(d_lanepw);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};

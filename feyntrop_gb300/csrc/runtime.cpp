@@ -29,18 +29,11 @@
 #include "problem.hpp"
 #include "xoshiro.hpp"
 
-namespace {
+#include "plan.hpp"
+
+namespace ftrt {
 
 thread_local std::string g_error;
-
-struct cuda_error : std::runtime_error {
-    using std::runtime_error::runtime_error;
-};
-
-void cu(cudaError_t e, const char* what)
-{
-    if (e != cudaSuccess) throw cuda_error(std::string(what) + ": " + cudaGetErrorString(e));
-}
 
 int status_of(const std::exception_ptr& ep)
 {
@@ -76,12 +69,6 @@ void require_device()
     }
 }
 
-// per-device constants: the 64 skip matrices T^(2^b)
-struct device_state {
-    unsigned long long* tpow = nullptr;
-    int sms = 0;
-};
-
 device_state& dev_state()
 {
     static std::mutex mu;
@@ -98,6 +85,27 @@ device_state& dev_state()
     }
     return d;
 }
+
+std::vector<double> param_block(const std::vector<double>& prm)
+{
+    const size_t n = prm.size();
+    std::vector<double> blk(n + (n + 1) / 2 + n, 0.0);
+    std::memcpy(blk.data(), prm.data(), n * 8);
+    float* f = (float*)(blk.data() + n);
+    for (size_t i = 0; i < n; i++) f[i] = (float)prm[i];
+    float* pd = (float*)(blk.data() + n + (n + 1) / 2);
+    for (size_t i = 0; i < n; i++) {
+        pd[2 * i] = (float)prm[i];
+        pd[2 * i + 1] = (float)(prm[i] - (double)pd[2 * i]);
+    }
+    return blk;
+}
+
+}  // namespace ftrt
+
+using namespace ftrt;
+
+namespace {
 
 // P~ = P restricted to vertices 0..V-2 (vertex V-1 is the deleted one), split as
 // sum_r sigma_r q_r q_r^T; eigenpairs with |sigma| <= 1e-14 max|sigma| are dropped
@@ -153,78 +161,8 @@ void low_rank(const ft::prepared& p, std::vector<double>& sigma, std::vector<dou
     }
 }
 
+
 }  // namespace
-
-struct ft_plan {
-    ft::prepared P;
-    std::vector<double> sigma, q, prm;
-    std::vector<unsigned char> tab;
-    int device = 0;
-    double* d_prm = nullptr;
-    unsigned char* d_tab = nullptr;
-    // scratch reused by launches
-    double* d_parts = nullptr;
-    size_t parts_cap = 0;
-    double* d_final = nullptr;
-    double* h_final = nullptr;
-    unsigned long long* d_queue = nullptr;
-    unsigned int* d_qcount = nullptr;
-    size_t qcap = 0;
-    unsigned long long* d_lanepw = nullptr;
-    unsigned long long lanepw_S = 0;
-    int lanepw_bits = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    std::mutex mu;
-    // launch shape of the sampling kernels (threads per block, minimum resident blocks
-    // per SM given to the register allocator), from a sweep on GB300: the mixed form
-    // gains ~1.6x on deformed integrals from 256 x 2 (168 registers instead of 255)
-    int tuned_block = 256, tuned_minb = 2;
-
-    ft::kernel_key key(int prec, int record) const
-    {
-        ft::kernel_key k;
-        k.E = P.E;
-        k.V = P.V;
-        k.K = P.K;
-        k.loops = P.loops;
-        k.rank = (int)sigma.size();
-        k.prec = prec;
-        k.mode = P.deformed() ? 1 : 0;
-        k.only_psi = P.only_psi() ? 1 : 0;
-        k.record = record;
-        k.block = tuned_block;
-        k.minb = prec == 0 ? 1 : tuned_minb;
-        if (const char* e = std::getenv("FEYNTROP_GB300_BLOCK")) k.block = std::atoi(e);
-        if (const char* e = std::getenv("FEYNTROP_GB300_MINB")) k.minb = std::atoi(e);
-        // out-of-line FP32 transcendentals pay off where the code is largest (deformed)
-        k.variant = P.deformed() ? 1 : 0;
-        if (const char* e = std::getenv("FEYNTROP_GB300_VARIANT")) k.variant = std::atoi(e);
-        k.ek = P.ek;
-        k.el = P.el;
-        // small tables are staged per block in shared memory; from E = 11 on the table is
-        // read through L1 (one cached copy per SM instead of one per block)
-        k.table_global = P.E >= 11 ? 1 : 0;
-        return k;
-    }
-
-    int slots() const { return 8 * P.K + 8; }
-
-    ~ft_plan()
-    {
-        if (d_prm) cudaFree(d_prm);
-        if (d_tab) cudaFree(d_tab);
-        if (d_parts) cudaFree(d_parts);
-        if (d_final) cudaFree(d_final);
-        if (h_final) cudaFreeHost(h_final);
-        if (d_queue) cudaFree(d_queue);
-        if (d_qcount) cudaFree(d_qcount);
-        if (d_lanepw) cudaFree(d_lanepw);
-        if (ev0) cudaEventDestroy(ev0);
-        if (ev1) cudaEventDestroy(ev1);
-        if (stream) cudaStreamDestroy(stream);
-    }
-};
 
 namespace {
 
@@ -270,21 +208,12 @@ void build_blocks(ft_plan& pl)
     }
 }
 
+// device copies and scratch of a plan, made on its first integration (a plan used only
+// through batches never allocates its own)
 void upload(ft_plan& pl)
 {
-    cu(cudaGetDevice(&pl.device), "cudaGetDevice");
-    // FP64 parameter block followed by the same values as floats
-    // FP64 block, then floats, then two-float (hi, lo) pairs
-    const size_t n = pl.prm.size();
-    std::vector<double> blk(n + (n + 1) / 2 + n, 0.0);
-    std::memcpy(blk.data(), pl.prm.data(), n * 8);
-    float* f = (float*)(blk.data() + n);
-    for (size_t i = 0; i < n; i++) f[i] = (float)pl.prm[i];
-    float* pd = (float*)(blk.data() + n + (n + 1) / 2);
-    for (size_t i = 0; i < n; i++) {
-        pd[2 * i] = (float)pl.prm[i];
-        pd[2 * i + 1] = (float)(pl.prm[i] - (double)pd[2 * i]);
-    }
+    if (pl.d_prm) return;
+    const std::vector<double> blk = param_block(pl.prm);
     cu(cudaMalloc(&pl.d_prm, blk.size() * 8), "cudaMalloc(params)");
     cu(cudaMalloc(&pl.d_tab, pl.tab.size()), "cudaMalloc(table)");
     cu(cudaMemcpy(pl.d_prm, blk.data(), blk.size() * 8, cudaMemcpyHostToDevice), "cudaMemcpy(params)");
@@ -442,6 +371,11 @@ run_out run(ft_plan& pl, const ft_run_options& o, cudaStream_t st, const records
     return out;
 }
 
+
+}  // namespace
+
+namespace ftrt {
+
 void fill_result(const ft::prepared& P, const std::vector<double>& acc, ft_result* r)
 {
     const int K = P.K;
@@ -465,7 +399,7 @@ void fill_result(const ft::prepared& P, const std::vector<double>& acc, ft_resul
     ft_finalize_moments(m.data(), K, P.deformed() ? 0 : 1, r);
 }
 
-}  // namespace
+}  // namespace ftrt
 
 static ft::problem_input input_of(const ft_problem* pb)
 {
@@ -525,7 +459,7 @@ int ft_plan_create(const ft_problem* pb, ft_plan** out)
         low_rank(pl->P, pl->sigma, pl->q);
         build_blocks(*pl);
         dev_state();
-        upload(*pl);
+        cu(cudaGetDevice(&pl->device), "cudaGetDevice");
         *out = pl.release();
         return FT_OK;
     } catch (const std::logic_error& e) {
@@ -576,8 +510,18 @@ int ft_precompile(const ft_problem* pb, int32_t precision, double* seconds)
         pl.P = ft::prepare(in);
         low_rank(pl.P, pl.sigma, pl.q);
         auto t0 = std::chrono::steady_clock::now();
-        ft::precompile(pl.key(0, 0));
-        if (precision == FT_PRECISION_MIXED) ft::precompile(pl.key(1, 0));
+        const int prec = precision & 0xff;
+        const bool batch = (precision & FT_PRECOMPILE_BATCH) != 0;
+        for (int bt = 0; bt <= (batch ? 1 : 0); bt++) {
+            ft::kernel_key k = pl.key(0, 0);
+            k.batch = bt;
+            ft::precompile(k);
+            if (prec == FT_PRECISION_MIXED) {
+                k = pl.key(1, 0);
+                k.batch = bt;
+                ft::precompile(k);
+            }
+        }
         if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return FT_OK;
     } catch (...) {
@@ -637,6 +581,7 @@ int ft_integrate(ft_plan* pl, const ft_run_options* o, ft_result* r)
         std::lock_guard<std::mutex> lock(pl->mu);
         auto t0 = std::chrono::steady_clock::now();
         cu(cudaSetDevice(pl->device), "cudaSetDevice");
+        upload(*pl);
         cudaStream_t st = o->stream ? (cudaStream_t)o->stream : pl->stream;
         run_out ro = run(*pl, *o, st, nullptr);
         fill_result(pl->P, ro.acc, r);
@@ -647,15 +592,6 @@ int ft_integrate(ft_plan* pl, const ft_run_options* o, ft_result* r)
     } catch (...) {
         return status_of(std::current_exception());
     }
-}
-
-int ft_integrate_batch(ft_plan* const* plans, int32_t count, const ft_run_options* opts, ft_result* results)
-{
-    for (int i = 0; i < count; i++) {
-        int rc = ft_integrate(plans[i], &opts[i], &results[i]);
-        if (rc != FT_OK) return rc;
-    }
-    return FT_OK;
 }
 
 int ft_integrate_noalloc(ft_plan* pl, const ft_run_options* o, double* d_slots)
@@ -669,7 +605,7 @@ int ft_integrate_noalloc(ft_plan* pl, const ft_run_options* o, double* d_slots)
             throw std::invalid_argument("ft_integrate_noalloc: more than 16 eps orders exceed the static scratch");
         const ft::kernel_set* ks = ft::find_kernels(pl->key(prec, 0));
         const ft::kernel_set* k64 = prec ? ft::find_kernels(pl->key(0, 0)) : nullptr;
-        if (!ks || (prec && !k64))
+        if (!ks || (prec && !k64) || !pl->d_prm)
             throw std::invalid_argument(
                 "ft_integrate_noalloc: this plan's kernels are not loaded; call ft_integrate once with the same "
                 "precision first (loading them allocates)");
@@ -727,6 +663,7 @@ int ft_sample_records(ft_plan* pl, const ft_run_options* o, uint8_t* order, doub
     try {
         std::lock_guard<std::mutex> lock(pl->mu);
         cu(cudaSetDevice(pl->device), "cudaSetDevice");
+        upload(*pl);
         const size_t N = o->num_samples, E = pl->P.E, K = pl->P.K;
         records d;
         cu(cudaMalloc(&d.order, N * E + 1), "cudaMalloc(records)");

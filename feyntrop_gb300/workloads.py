@@ -10,7 +10,7 @@ import math
 import random
 
 __all__ = ["k4_euclidean", "double_box", "box_pentagon", "cube_propagator", "ladder3", "wheel4_vacuum",
-           "triangle", "kinematic_matrix"]
+           "triangle", "kinematic_matrix", "log_uniform_n", "box_pentagon_scan", "mixed_batch"]
 
 
 def kinematic_matrix(V, sp):
@@ -57,11 +57,15 @@ BOX_PENTAGON_EDGES = [[[0, 1], 1], [[1, 2], 1], [[2, 6], 1], [[6, 3], 1], [[3, 4
                       [[5, 6], 1]]
 
 
-def box_pentagon(rng, D=6, K=3, nmin=1e5, nmax=1e7):
+def log_uniform_n(rng, nmin, nmax):
+    return int(math.exp(rng.uniform(math.log(nmin), math.log(nmax))))
+
+
+def box_pentagon(rng, D=6, K=3, nmin=1e5, nmax=1e7, mmax=2.0):
     """Box-pentagon topology of the reference's test suite (7 vertices, 8 edges,
-    externals 0-4) with masses U[0, 2], the 10 independent invariants U[-10, 10],
+    externals 0-4) with masses U[0, mmax], the 10 independent invariants U[-10, 10],
     lambda U[0.2, 1.0] and N log-uniform in [nmin, nmax]."""
-    m2 = [rng.uniform(0, 2) for _ in range(8)]
+    m2 = [rng.uniform(0, mmax) for _ in range(8)]
     inv = [rng.uniform(-10, 10) for _ in range(10)]
     lam = rng.uniform(0.2, 1.0)
     N = int(math.exp(rng.uniform(math.log(nmin), math.log(nmax))))
@@ -131,3 +135,50 @@ def triangle(rng, nmin=1e5, nmax=1e8, K=3):
     sp = {(0, 0): pp0, (1, 1): pp1, (0, 1): (s01 - pp0 - pp1) / 2}
     N = int(math.exp(rng.uniform(math.log(nmin), math.log(nmax))))
     return _inp([[[0, 1], 1], [[1, 2], 1], [[2, 0], 1]], 4, kinematic_matrix(3, sp), m2, K, 0, N)
+
+
+def _accepted(make, accept):
+    """make() until accept(inp) holds; returns (inp, number of rejected draws)."""
+    rejected = 0
+    while True:
+        inp = make()
+        if accept is None or accept(inp):
+            return inp, rejected
+        rejected += 1
+
+
+def box_pentagon_scan(count=4096, seed=3, accept=None):
+    """Batched kinematic scan: `count` box-pentagon instances drawn from
+    random.Random(seed) (masses U[0, 2], invariants U[-10, 10], lambda U[0.2, 1],
+    N log-uniform in [1e5, 1e7]).  An instance that accept() rejects (the plan's own
+    input checks: non-generic or divergent points) is redrawn from the same generator.
+    Returns (inputs, number of redrawn instances)."""
+    rng = random.Random(seed)
+    out, redrawn = [], 0
+    for _ in range(count):
+        inp, r = _accepted(lambda: box_pentagon(rng), accept)
+        out.append(inp)
+        redrawn += r
+    return out, redrawn
+
+
+def mixed_batch(seed=5, counts=(512, 512, 256, 256), nmin=1e5, nmax=1e8, accept=None):
+    """Mixed uneven batch: counts[0] 1-loop triangles (Euclidean), counts[1] 3-loop
+    4-point ladders (alternately Euclidean and Minkowski), counts[2] 4-loop wheel vacuum
+    graphs (all masses 1) and counts[3] box-pentagons (Minkowski), masses U[0, 3], every
+    instance with N log-uniform in [nmin, nmax], all from random.Random(seed).  Returns
+    (inputs, number of redrawn instances)."""
+    rng = random.Random(seed)
+    out, redrawn = [], 0
+    makers = [
+        lambda k: triangle(rng, nmin, nmax),
+        lambda k: ladder3(rng, euclidean=(k % 2 == 0), nmin=nmin, nmax=nmax),
+        lambda k: wheel4_vacuum(N=log_uniform_n(rng, nmin, nmax)),
+        lambda k: box_pentagon(rng, nmin=nmin, nmax=nmax, mmax=3.0),
+    ]
+    for kind, n in enumerate(counts):
+        for k in range(n):
+            inp, r = _accepted(lambda: makers[kind](k), accept)
+            out.append(inp)
+            redrawn += r
+    return out, redrawn

@@ -109,8 +109,40 @@ typedef struct {
  * of the reference run with OMP_NUM_THREADS=1. */
 int ft_integrate(ft_plan* plan, const ft_run_options* opts, ft_result* result);
 
-/* Several plans in one call (one launch per plan today, all on one stream). */
+/* Several integrals in one call: a batch (below) created, run once and destroyed.  Plans
+ * with FT_PRECISION_MIXED options form one batch, the others a second.  Each result is
+ * that of ft_integrate with the same options, up to the order of the sums.  The
+ * reference integrates one graph per process (srcs/feyntrop.cpp:251); this is the
+ * in-process counterpart of running it once per kinematic point. */
 int ft_integrate_batch(ft_plan* const* plans, int32_t count, const ft_run_options* opts, ft_result* results);
+
+/* A batch: many integrals (any mix of graphs, kinematics, seeds and sample counts) run
+ * by one CUDA graph launch.  Integrals of one kernel class (same topology, eps orders,
+ * regime) share one persistent sampling launch whose blocks take work items of
+ * consecutive samples from a device counter; classes run side by side.  The batch
+ * copies the plans' parameters and tables at creation; the plans must outlive it (their
+ * host data finalises the results).  Reusable: ft_batch_run may be called any number of
+ * times with new sample counts, seeds and first samples; the graph is captured on the
+ * first run and again only when a run needs more work items or FP64 hand-off entries
+ * than the previous ones.  precision applies to every integral of the batch. */
+typedef struct ft_batch ft_batch;
+int ft_batch_create(ft_plan* const* plans, int32_t count, int32_t precision, ft_batch** out);
+void ft_batch_destroy(ft_batch* batch);
+/* opts[i] (num_samples, seed, first_sample) for integral i; opts[0].stream (or NULL for
+ * the batch's own stream) carries the graph launch; precision fields are ignored.
+ * results[i] as from ft_integrate; kernel_ms is the whole graph's device time. */
+int ft_batch_run(ft_batch* batch, const ft_run_options* opts, ft_result* results);
+
+typedef struct {
+    int32_t num_integrals;
+    int32_t num_classes;         /* persistent sampling launches per run */
+    int32_t graph_captures;      /* captures so far */
+    int32_t kernel_launches;     /* kernel nodes of the graph */
+    uint64_t work_items;         /* of the last run */
+    uint64_t fp64_queue_capacity;
+    double kernel_ms;            /* device time of the last run (CUDA events) */
+} ft_batch_info;
+int ft_batch_get_info(const ft_batch* batch, ft_batch_info* info);
 
 /* Integration that allocates no memory, for callers that must not allocate device
  * memory while they integrate (an embedding application or serving loop that owns all
@@ -152,8 +184,10 @@ int ft_subgraph_table(const ft_problem* problem, double* Jr, double* r, uint8_t*
                       ft_plan_info* info);
 
 /* Host preprocessing plus run-time compilation of the sampling kernels for this
- * problem's topology (FP64 and, if requested, mixed), without touching a device:
- * warms the kernel cache.  *seconds receives the compile time (0 when cached). */
+ * problem's topology (FP64 and, if requested, mixed; with FT_PRECOMPILE_BATCH or'ed
+ * into precision also the batch kernels), without touching a device: warms the kernel
+ * cache.  *seconds receives the compile time (0 when cached). */
+#define FT_PRECOMPILE_BATCH 0x100
 int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds);
 
 /* Measured FP32 and FP64 FMA issue rates of the current device in TFLOP/s (an

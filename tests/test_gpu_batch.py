@@ -1,0 +1,137 @@
+"""Batches (ft_batch_*, ft_integrate_batch): many integrals of several topologies in
+one CUDA graph launch, against ft_integrate of each integral on the same samples.
+
+Each integral of a batch walks the same sample stream as ft_integrate with the same
+seed and first sample, so the counts of kept, dropped and FP64-re-evaluated samples
+agree exactly and the averages agree to the rounding of the sums (their order
+differs): to 1e-6 of a standard error in FP64, 1e-3 in mixed precision (the FP32
+partial sums of 256 samples round differently when the samples are grouped
+differently).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import feyntrop_gb300 as ft
+from feyntrop_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+PINS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_pins.json")))
+NAMES = ["C1_K4", "C2_double_box", "2L_5pt_box_pent", "C3_box_pentagon_0", "1L_3pt_eucl", "2L_3pt_tutorial",
+         "wheel4_vacuum"]
+TOL = {ft.FP64: 1e-6, ft.MIXED: 1e-3}
+
+
+def assert_same(b, r, precision, what):
+    assert b["kept"] == r["kept"] and b["dropped"] == r["dropped"], what
+    assert b["fp64_fallback"] == r["fp64_fallback"] and b["exact_steps"] == r["exact_steps"], what
+    for j, ((re, dre), (im, dim)) in enumerate(r["integral"]):
+        (bre, bdre), (bim, bdim) = b["integral"][j]
+        assert abs(bre - re) <= TOL[precision] * dre, (what, j, bre, re, dre)
+        assert abs(bdre - dre) <= 1e-3 * dre, (what, j, bdre, dre)
+        if dim == 0:
+            assert bim == 0 and bdim == 0, what
+        else:
+            assert abs(bim - im) <= TOL[precision] * dim, (what, j, bim, im, dim)
+
+
+@pytest.fixture(scope="module")
+def plans():
+    ps = [ft.Plan(PINS["cases"][n]["input"]) for n in NAMES]
+    yield ps
+    for p in ps:
+        p.close()
+
+
+@pytest.mark.parametrize("precision", [ft.FP64, ft.MIXED])
+def test_batch_equals_single_integrals(plans, precision):
+    Ns = [1_500_000, 700_001, 1_000_003, 333_333, 2_000_000, 123_457, 999_999]
+    seeds = [0, 1, 2, 3, 4, 5, 6]
+    b = ft.Batch(plans, precision)
+    out = b.run(Ns, seeds)
+    info = b.info()
+    assert info["num_integrals"] == len(plans)
+    assert info["num_classes"] == len(set(NAMES))   # all topologies differ here
+    for i, p in enumerate(plans):
+        r = p.integrate(Ns[i], seed=seeds[i], precision=precision)
+        assert_same(out[i], r, precision, NAMES[i])
+    b.close()
+
+
+def test_batch_is_reusable_with_new_seeds_and_offsets(plans):
+    b = ft.Batch(plans, ft.MIXED)
+    b.run(200_000, seeds=1)
+    captures = b.info()["graph_captures"]
+    out = b.run(150_000, seeds=9, first_samples=[0, 10, 20, 30, 40, 50, 60])
+    assert b.info()["graph_captures"] == captures   # fewer items than before: graph replayed
+    for i, p in enumerate(plans):
+        r = p.integrate(150_000, seed=9, precision=ft.MIXED, first_sample=10 * i)
+        assert_same(out[i], r, ft.MIXED, NAMES[i])
+    out = b.run(2_500_000, seeds=2)           # more items: buffers grow, graph recaptured
+    assert b.info()["graph_captures"] == captures + 1
+    r = plans[1].integrate(2_500_000, seed=2, precision=ft.MIXED)
+    assert_same(out[1], r, ft.MIXED, NAMES[1])
+    b.close()
+
+
+def test_integrate_batch_splits_precisions(plans):
+    ps = plans[:4]
+    N = [300_000] * 4
+    precs = [ft.FP64, ft.MIXED, ft.MIXED, ft.FP64]
+    n = len(ps)
+    import ctypes
+    arr = (ctypes.c_void_p * n)(*[p.h.value for p in ps])
+    opts = (ft.RunOptions * n)(*[ft.RunOptions(N[i], 3, 0, precs[i], None) for i in range(n)])
+    ras = [ft._ResultArrays(p.K) for p in ps]
+    res = (ft.Result * n)(*[r.res for r in ras])
+    rc = ft.lib().ft_integrate_batch(ctypes.cast(arr, ctypes.c_void_p), n, ctypes.cast(opts, ctypes.c_void_p),
+                                     ctypes.cast(res, ctypes.c_void_p))
+    assert rc == ft.FT_OK, ft.lib().ft_last_error()
+    for i, p in enumerate(ps):
+        ras[i].res = res[i]
+        b = ras[i].as_dict(p.info["IGtr"])
+        r = p.integrate(N[i], seed=3, precision=precs[i])
+        assert_same(b, r, precs[i], NAMES[i])
+
+
+def test_kinematic_scan_batch():
+    """64 random box-pentagon points (their own masses, invariants, lambda and N) in one
+    persistent launch, each against its own ft_integrate."""
+    def accept(inp):
+        try:
+            ft.subgraph_table(inp)
+            return True
+        except ft.FeyntropError:
+            return False
+
+    inputs, _ = workloads.box_pentagon_scan(64, seed=11, accept=accept)
+    ps = [ft.Plan(x) for x in inputs]
+    Ns = [min(x["N"], 400_000) for x in inputs]
+    b = ft.Batch(ps, ft.MIXED)
+    out = b.run(Ns, seeds=list(range(64)))
+    classes = b.info()["num_classes"]
+    assert classes <= 2    # deformed, and possibly a pseudo-Euclidean point
+    for i, p in enumerate(ps):
+        r = p.integrate(Ns[i], seed=i, precision=ft.MIXED)
+        assert_same(out[i], r, ft.MIXED, "scan %d" % i)
+    b.close()
+    for p in ps:
+        p.close()
+
+
+def test_batch_matches_reference_aggregates():
+    """The reference's own N = 2e5 aggregates (same samples, seed 0) through a batch."""
+    names = ["1L_2pt", "1L_3pt_mink", "2L_4pt_ladder", "C4_cube", "K4_masses_1to6"]
+    ps = [ft.Plan(PINS["cases"][n]["input"]) for n in names]
+    N = PINS["N_aggregate"]
+    out = ft.Batch(ps, ft.FP64).run(N, seeds=0)
+    for i, n in enumerate(names):
+        for j, ((re, dre), (im, dim)) in enumerate(PINS["cases"][n]["aggregate"]["integral"]):
+            g_re, g_dre = out[i]["integral"][j][0]
+            assert abs(g_re - re) <= 1e-6 * dre, (n, j, g_re, re)
+            assert abs(g_dre - dre) <= 1e-6 * dre
+    for p in ps:
+        p.close()

@@ -118,3 +118,33 @@ def test_no_cpu_fallback_without_a_device():
     with pytest.raises(ft.FeyntropError) as e:
         ft.Plan(workloads.k4_euclidean())
     assert e.value.code == ft.FT_ERR_NO_DEVICE
+
+
+def test_batch_api_rejects_bad_arguments_without_a_device():
+    import ctypes
+    L = ft.lib()
+    h = ctypes.c_void_p()
+    assert L.ft_batch_create(None, 0, ft.MIXED, ctypes.byref(h)) == ft.FT_ERR_INVALID_ARGUMENT
+    assert "no plans" in L.ft_last_error().decode()
+    arr = (ctypes.c_void_p * 1)(None)
+    assert L.ft_batch_create(ctypes.cast(arr, ctypes.c_void_p), 1, 7, ctypes.byref(h)) == ft.FT_ERR_INVALID_ARGUMENT
+    assert h.value is None
+
+
+def test_batch_workloads_are_seeded_and_redraw_rejected_points():
+    from feyntrop_gb300 import workloads as w
+    a, _ = w.box_pentagon_scan(16, seed=3)
+    b, _ = w.box_pentagon_scan(16, seed=3)
+    assert a == b
+    assert all(1e5 <= x["N"] <= 1e7 for x in a)
+    calls = []
+
+    def reject_every_other(inp):
+        calls.append(1)
+        return len(calls) % 2 == 0
+
+    c, redrawn = w.box_pentagon_scan(8, seed=3, accept=reject_every_other)
+    assert redrawn == 8 and len(c) == 8
+    m, _ = w.mixed_batch(seed=5, counts=(4, 4, 2, 2))
+    assert [len(x["graph"]) for x in m] == [3] * 4 + [10] * 4 + [8] * 2 + [8] * 2
+    assert [x["lambda"] for x in m[4:8]] == [0, 0.5, 0, 0.5]
