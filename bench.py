@@ -16,6 +16,11 @@ reported time is the max over ranks.  `e2e` repeats the step through the public
 API as a user calls it (plan creation with host preprocessing and the upload of
 the table, integration, result read-back) timed on the host.
 
+Batched form (`batched` in the line, --batched scan|mixed|none): a whole seeded batch
+of integrals (4096 box-pentagon kinematic points by default) per run, one CUDA graph
+launch with one persistent sampling launch per topology class, mixed precision
+against plain FP64 on the same integrals.
+
 Multi-GPU (torchrun): rank r integrates its own block of N samples of the same
 stream (samples [rN, (r+1)N)); the merged moments equal a single run over all
 blocks; weak scaling.
@@ -153,6 +158,91 @@ def cpu_rate(inp, seconds, threads, kind_pref=("reference", "port")):
     return n / (time.perf_counter() - t0), n, "port"
 
 
+def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
+    """The batched form: every integral of a seeded batch in one CUDA graph launch per
+    run (ft_batch_*), mixed precision against plain FP64 on the same integrals.
+
+    scan:  4096 box-pentagon kinematic points (masses U[0, 2], invariants U[-10, 10],
+           lambda U[0.2, 1], N log-uniform in [1e5, 1e7], Random(3)), about 9e9 samples;
+    mixed: 512 triangles, 512 3-loop ladders, 256 4-loop vacuum wheels, 256
+           box-pentagons (N log-uniform in [1e5, 1e8], Random(5)), about 2.2e10 samples.
+    The FP64 runs use every integral's N times --batch-fp64-scale (the rate does not
+    depend on it while the work items outnumber the GPU's block slots).  One warm-up run
+    per precision (graph capture), then --batch-steps timed runs with an L2 flush
+    between them, timed with CUDA events around the graph launch on its stream."""
+    def accept(inp):
+        try:
+            ft.subgraph_table(inp)
+            return True
+        except ft.FeyntropError:
+            return False
+
+    if args.batched == "scan":
+        inputs, redrawn = workloads.box_pentagon_scan(4096, seed=3, accept=accept)
+        name = ("box-pentagon kinematic scan: 4096 points (7 vertices, 8 edges, D=6, 3 eps orders), masses U[0,2], "
+                "invariants U[-10,10], lambda U[0.2,1], N log-uniform [1e5,1e7], Random(3)")
+    else:
+        inputs, redrawn = workloads.mixed_batch(seed=5, accept=accept)
+        name = ("mixed uneven batch: 512 triangles, 512 3-loop ladders, 256 4-loop vacuum wheels, 256 box-pentagons, "
+                "masses U[0,3], N log-uniform [1e5,1e8], Random(5)")
+    t0 = time.perf_counter()
+    plans = ft.create_plans(inputs)
+    t_plans = time.perf_counter() - t0
+    Ns = [x["N"] for x in inputs]
+    stream = torch.cuda.Stream()
+    out = {"workload": name, "integrals": len(plans), "redrawn": redrawn, "samples_per_run": sum(Ns),
+           "seconds_preprocessing_all": t_plans}
+    rates = {}
+    for prec, scale, tag in ((ft.MIXED, 1.0, "mixed"), (ft.FP64, args.batch_fp64_scale, "plain_fp64")):
+        t0 = time.perf_counter()
+        b = ft.Batch(plans, prec)
+        t_create = time.perf_counter() - t0
+        n = [max(1, int(x * scale)) for x in Ns]
+        times, res = [], None
+        with clocks_sampler() as clk:
+            for step in range(1 + args.batch_steps):
+                flush.fill_(float(step))
+                torch.cuda.synchronize()
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                res = b.run(n, seeds=step, stream=stream.cuda_stream)
+                ev1.record(stream)
+                ev1.synchronize()
+                if step >= 1:
+                    times.append(ev0.elapsed_time(ev1))
+        info = b.info()
+        ms = sum(times) / len(times)
+        rates[tag] = sum(n) / (ms * 1e-3)
+        out[tag] = {"value": rates[tag], "unit": UNIT, "ms_per_run": ms, "runs": len(times),
+                    "sample_scale": scale, "samples_per_run": sum(n), "classes": info["num_classes"],
+                    "kernel_launches_per_run": info["kernel_launches"], "graph_launches_per_run": 1,
+                    "graph_captures": info["graph_captures"], "work_items": info["work_items"],
+                    "seconds_batch_create": t_create, "clocks": clk.summary()}
+        if prec == ft.MIXED:
+            out[tag]["fp64_fallback_rate"] = sum(r["fp64_fallback"] for r in res) / sum(n)
+            out["e2e_mixed"] = {"value": sum(n) / (t_plans + t_create + ms * 1e-3), "unit": UNIT,
+                                "includes": "host preprocessing of every integral, batch creation, one run"}
+        b.close()
+    out["mixed_over_fp64"] = rates["mixed"] / rates["plain_fp64"]
+    # per-sample error of the mixed form against the FP64 form on the first 8 integrals
+    import numpy as np
+    errs = []
+    for p in plans[:8]:
+        rm = p.records(1 << 14, seed=0, precision=ft.MIXED)
+        r6 = p.records(1 << 14, seed=0, precision=ft.FP64)
+        ok = (r6["flags"] & 1) == 0
+        scale_ = np.abs(r6["R"][ok]).max(axis=1)
+        e = np.abs(rm["R"][ok] - r6["R"][ok]).max(axis=1) / np.where(scale_ > 0, scale_, 1.0)
+        errs.append(e)
+    e = np.concatenate(errs)
+    out["per_sample_error"] = {"samples": int(e.size), "max": float(e.max()), "mean": float(e.mean()),
+                               "p99.9": float(np.quantile(e, 0.999)), "frac_above_1e-5": float((e > 1e-5).mean()),
+                               "against": "the plain-FP64 GPU form, first 8 integrals x 16384 samples"}
+    for p in plans:
+        p.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -193,6 +283,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", action="store_true",
                     help="only the timed sampling steps (for profiler captures); prints a reduced line")
+    ap.add_argument("--batched", default="scan", choices=["scan", "mixed", "none"],
+                    help="the batched form's workload (one GPU runs it, rank 0 reports it)")
+    ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--batch-fp64-scale", type=float, default=1 / 16)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -322,6 +416,9 @@ def main():
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": "%d samples of the double-box workload (same stream), all host threads" % nsample}
     traffic = dram_traffic("ft_sample mixed double_box")
+    batched = None
+    if args.batched != "none" and rank == 0:
+        batched = batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -349,6 +446,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clocks,
         "cpu_baseline": cpu,
+        "batched": batched,
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -35,7 +35,8 @@ MIXED = 1
 EXPORTED = ["ft_plan_create", "ft_plan_destroy", "ft_plan_get_info", "ft_plan_log_line", "ft_integrate",
             "ft_integrate_batch", "ft_finalize_moments", "ft_sample_records", "ft_run_json", "ft_free",
             "ft_precompile", "ft_last_error", "ft_version", "ft_subgraph_table", "ft_device_peaks", "ft_integrate_noalloc",
-            "ft_batch_create", "ft_batch_destroy", "ft_batch_run", "ft_batch_get_info"]
+            "ft_batch_create", "ft_batch_destroy", "ft_batch_run", "ft_batch_get_info", "ft_plans_create",
+            "ft_autotune"]
 PRECOMPILE_BATCH = 0x100
 
 
@@ -78,6 +79,12 @@ class Result(ctypes.Structure):
                 ("seconds_sampling", ctypes.c_double), ("kernel_launches", ctypes.c_int32)]
 
 
+class TuneResult(ctypes.Structure):
+    _fields_ = [("block", ctypes.c_int32), ("min_blocks_per_sm", ctypes.c_int32), ("variant", ctypes.c_int32),
+                ("samples_per_second", ctypes.c_double), ("default_samples_per_second", ctypes.c_double),
+                ("candidates", ctypes.c_int32)]
+
+
 class BatchInfo(ctypes.Structure):
     _fields_ = [("num_integrals", ctypes.c_int32), ("num_classes", ctypes.c_int32),
                 ("graph_captures", ctypes.c_int32), ("kernel_launches", ctypes.c_int32),
@@ -116,6 +123,8 @@ def lib():
             L.ft_precompile.argtypes = [ctypes.POINTER(Problem), ctypes.c_int32, ctypes.POINTER(ctypes.c_double)]
             L.ft_integrate_noalloc.argtypes = [ctypes.c_void_p, ctypes.POINTER(RunOptions), ctypes.c_void_p]
             L.ft_device_peaks.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+            L.ft_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint64, ctypes.POINTER(TuneResult)]
+            L.ft_plans_create.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
             L.ft_batch_create.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32,
                                           ctypes.POINTER(ctypes.c_void_p)]
             L.ft_batch_destroy.argtypes = [ctypes.c_void_p]
@@ -184,11 +193,14 @@ def precompile(inp, precision=MIXED):
 class Plan:
     """One integral on the GPU (host preprocessing + device tables)."""
 
-    def __init__(self, inp):
-        self.arrays = _ProblemArrays(inp)
+    def __init__(self, inp, _handle=None):
+        self.arrays = inp if isinstance(inp, _ProblemArrays) else _ProblemArrays(inp)
         self.E, self.V, self.K = self.arrays.E, self.arrays.V, self.arrays.K
-        h = ctypes.c_void_p()
-        _check(lib().ft_plan_create(ctypes.byref(self.arrays.struct), ctypes.byref(h)))
+        if _handle is None:
+            h = ctypes.c_void_p()
+            _check(lib().ft_plan_create(ctypes.byref(self.arrays.struct), ctypes.byref(h)))
+        else:
+            h = _handle
         self.h = h
         info = PlanInfo()
         _check(lib().ft_plan_get_info(self.h, ctypes.byref(info)))
@@ -223,6 +235,13 @@ class Plan:
             "seconds_sampling": res.seconds_sampling, "kernel_launches": res.kernel_launches,
         }
 
+    def autotune(self, precision=MIXED, samples=2_000_000):
+        """Time this plan's kernel class under candidate launch shapes and record the
+        fastest in the tuning table (used by every later plan and batch of the class)."""
+        t = TuneResult()
+        _check(lib().ft_autotune(self.h, int(precision), int(samples), ctypes.byref(t)))
+        return {f: getattr(t, f) for f, _ in TuneResult._fields_}
+
     def records(self, count, seed=0, first_sample=0, precision=FP64):
         """Per-sample records of samples first_sample .. first_sample+count-1."""
         E, K = self.E, self.K
@@ -233,6 +252,25 @@ class Plan:
         opts = RunOptions(int(count), int(seed), int(first_sample), int(precision), None)
         _check(lib().ft_sample_records(self.h, ctypes.byref(opts), _ptr(order), _ptr(X), _ptr(R), _ptr(flags)))
         return {"order": order.astype(np.int32), "X": X, "R": R[..., 0] + 1j * R[..., 1], "flags": flags}
+
+
+def create_plans(inputs, skip_failed=False):
+    """Plans for many inputs at once (ft_plans_create: host preprocessing on all host
+    threads).  A failing input raises FeyntropError, or gives None with skip_failed."""
+    arrays = [_ProblemArrays(x) for x in inputs]
+    n = len(arrays)
+    probs = (Problem * n)(*[a.struct for a in arrays])
+    hs = (ctypes.c_void_p * n)()
+    st = (ctypes.c_int32 * n)()
+    rc = lib().ft_plans_create(ctypes.cast(probs, ctypes.c_void_p), n, ctypes.cast(hs, ctypes.c_void_p),
+                               ctypes.cast(st, ctypes.c_void_p))
+    if rc != FT_OK and not skip_failed:
+        msg = lib().ft_last_error().decode(errors="replace")
+        for h in hs:
+            if h:
+                lib().ft_plan_destroy(ctypes.c_void_p(h))
+        raise FeyntropError(rc, msg)
+    return [Plan(a, _handle=ctypes.c_void_p(h)) if h else None for a, h in zip(arrays, hs)]
 
 
 class _ResultArrays:

@@ -25,7 +25,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-SOURCES = ["json.cpp", "problem.cpp", "xoshiro.cpp", "jit.cpp", "runtime.cpp", "batch.cpp", "driver.cpp"]
+SOURCES = ["json.cpp", "problem.cpp", "xoshiro.cpp", "jit.cpp", "runtime.cpp", "batch.cpp", "tune.cpp", "driver.cpp"]
 LIB = os.path.join(OUT, "libfeyntrop_gb300.so")
 CLI = os.path.join(OUT, "feyntrop")
 

@@ -201,7 +201,8 @@ void build(ft_batch& b)
             k64.batch = 1;
             g.k64 = &ft::get_kernels(k64);
         }
-        g.chunk = env_u64("FEYNTROP_GB300_BATCH_CHUNK", prec ? 64 : 16);
+        const ft::launch_shape tuned = ft::choose_shape(g.key);
+        g.chunk = env_u64("FEYNTROP_GB300_BATCH_CHUNK", tuned.chunk ? tuned.chunk : (prec ? 64 : 16));
         if (g.chunk < 1 || g.chunk >= (1ull << 18)) throw std::invalid_argument("batch chunk out of range");
         g.lanebits = 1;
         while ((1 << g.lanebits) < g.ks->block) g.lanebits++;
@@ -438,7 +439,7 @@ int ft_batch_run(ft_batch* b, const ft_run_options* opts, ft_result* results)
                 p->first_item = next;
                 p->nitems = items;
                 next += items;
-                q += (size_t)std::min<unsigned long long>(N, N / 128 + 1024);
+                q += (size_t)std::min<unsigned long long>(N, N / 64 + 1024);
             }
             if (next >= (1ull << 36)) throw std::invalid_argument("ft_batch_run: too many work items");
             g.total_items = next;

@@ -60,7 +60,7 @@ static uint64_t fnv1a(const std::string& s)
     return h;
 }
 
-static std::string cache_dir()
+std::string cache_dir()
 {
     if (const char* env = std::getenv("FEYNTROP_GB300_CACHE")) return env;
     Dl_info info;

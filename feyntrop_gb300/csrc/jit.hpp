@@ -43,6 +43,9 @@ struct kernel_set {
 
 std::string kernel_source(const kernel_key& key);
 
+// directory of the compiled-kernel cache (and of the launch-shape tuning table)
+std::string cache_dir();
+
 // shared memory the kernel stages the table into (0 when read from global memory)
 unsigned table_smem_bytes(const kernel_key& key);
 

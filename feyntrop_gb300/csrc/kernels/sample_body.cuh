@@ -63,7 +63,9 @@ typedef unsigned int u32;
 // that the small matrices stay in registers), and the FP32 library functions carry
 // large slow paths.  FT_VARIANT bit 0 keeps one out-of-line copy of each FP32
 // transcendental, bit 1 does the same for the two-float primitives, so the code the
-// SM streams per sample fits the instruction caches better.
+// SM streams per sample fits the instruction caches better; bit 2 starts every sample
+// with a block-wide barrier, so that the block's warps walk the code together and
+// share its instruction fetches.
 #ifndef FT_VARIANT
 #define FT_VARIANT 0
 #endif
@@ -944,7 +946,9 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
         }
     }
     auto Gx = [&](int i, int j) -> df { return (i == FT_V - 1 || j == FT_V - 1) ? df_mk(0.0f) : G[i][j]; };
-    const float kappa = pd[2 * P_DEF];
+    df kappa;
+    kappa.hi = pd[2 * P_DEF];
+    kappa.lo = pd[2 * P_DEF + 1];
 #pragma unroll
     for (int a2 = 0; a2 < FT_E; a2++) {
         const int ka = FT_EK[a2], la = FT_EL[a2];
@@ -965,7 +969,7 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
         df m2;
         m2.hi = pd[2 * (P_M2 + a2)];
         m2.lo = pd[2 * (P_M2 + a2) + 1];
-        theta_out[a2] = df_mul(df_sub(m2, xas), df_mk(kappa));
+        theta_out[a2] = df_mul(df_sub(m2, xas), kappa);
         // 2 xa s (1/x - xa t)
         H_out[a2][a2] = 2.0f * df_f(df_mul(xas, df_sub(xi, df_mul(xa, t))));
 #pragma unroll
@@ -1036,6 +1040,18 @@ static __device__ __forceinline__ f2 f2_neg(f2 a) { return f2_make(-a.hi, -a.lo)
 #ifndef PIVOT_GROWTH
 #define PIVOT_GROWTH 0.03f
 #endif
+// largest accepted (D/2) det L(|y|) / |det L(y)|: the complex determinant is a sum over
+// spanning trees with phases, and FP32 errors in it (and in psi^(-D/2)) grow by the
+// ratio of the phase-free sum to the result
+#ifndef DET_CANCEL
+#define DET_CANCEL 160.0f
+#endif
+// largest accepted W (sum |terms of V|) / (|V| pivot growth) in the deformed integrand:
+// V^(-W) carries the FP32 error of the complex solves (grown by 1 / pivot growth),
+// amplified by the cancellation in V
+#ifndef V_AMPLIFY
+#define V_AMPLIFY 160.0f
+#endif
 #define RLN2_HI 1.44269502162933349609375f
 #define RLN2_LO 1.925963033500011e-8f
 #define LN2_F 0.69314718055994531f
@@ -1065,7 +1081,10 @@ static __device__ __forceinline__ f2 wrap_pi2(f2 x, bool& edge)
 {
     const float TWO_PI_HI = 6.28318548202514648f, TWO_PI_LO = -1.7484555e-7f;
     const float k = rintf((x.hi + x.lo) * 0.159154943091895336f);
-    f2 r = f2_add(x, -k * TWO_PI_HI);
+    // k * 2pi as an exact two-float product (k * TWO_PI_HI alone is rounded once |k| > 1)
+    const float p = k * TWO_PI_HI;
+    f2 r = f2_add(x, -p);
+    r = f2_add(r, -fmaf(k, TWO_PI_HI, -p));
     r = f2_add(r, -k * TWO_PI_LO);
     edge |= fabsf(r.hi + r.lo) > 3.14158265f;
     return r;
@@ -1192,6 +1211,14 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
         const float im = rcp_(m);
         ph = ph * cmk(CL.d[k].re * im, CL.d[k].im * im);
     }
+    {
+        const int de = min(max(psi.e - cpsi.e, -100), 100);
+        const float rho = psi.m / cpsi.m * __int_as_float((127 + de) << 23);
+        if (!(D2 * rho < DET_CANCEL)) {
+            need64 = true;
+            return false;
+        }
+    }
     bool edge = false;
     // arg cPsi = sum theta + arg det, reduced to the principal branch in two-float
     const f2 apsi2 = wrap_pi2(f2_add(thsum, m_atan2(ph.im, ph.re)), edge);
@@ -1218,7 +1245,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     FT_DBG(23, cpphi.im);
     // V cancels near thresholds: its FP32 error is ~ 1e-7 * mag / |V|, so samples where
     // |V| < V_CANCEL * mag go to the FP64 pass
-    if (!(vabs > V_CANCEL * mag)) {
+    if (!(vabs > V_CANCEL * mag) || !(W * mag < V_AMPLIFY * growth * vabs)) {
         need64 = true;
         return false;
     }
@@ -1261,6 +1288,10 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     FT_DBG(25, atan2f(pj.im, pj.re));
     FT_DBG(26, apsi);
     FT_DBG(27, growth);
+    FT_DBG(28, mag / vabs);
+    FT_DBG(29, jgrowth);
+    FT_DBG(30, thsum.hi);
+    FT_DBG(31, (float)(cpsi.e - psi.e) + log2f(cpsi.m / psi.m));
     if (edge || cpsi.bad || mv.bad || mj.bad || !(jgrowth > PIVOT_GROWTH)) {
         need64 = true;
         return false;
@@ -1661,7 +1692,7 @@ static __device__ __forceinline__ void sample64(xo& g, const table_ref& tr, cons
 // single-integral kernels, one word `qtag | (i - first)` in the batch kernels (the
 // FP64 pass re-derives the state from the work item).
 static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, const double* __restrict__ prm,
-                                                    u64 first, u64 last, accum& A, u64* __restrict__ queue,
+                                                    u64 first, u64 last, u64 chunk, accum& A, u64* __restrict__ queue,
                                                     unsigned int* __restrict__ qcount, unsigned int qcap, u64 qtag,
                                                     unsigned char* __restrict__ rec_order, double* __restrict__ rec_X,
                                                     double* __restrict__ rec_R, unsigned char* __restrict__ rec_flags)
@@ -1671,7 +1702,18 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
     const float* pd = (const float*)(prm + P_SIZE + (P_SIZE + 1) / 2);   // two-float pairs
 #endif
     (void)qtag;
+    (void)chunk;
+#if FT_VARIANT & 4
+    // Every thread of the block makes `chunk` trips and the block starts each sample
+    // together: the warps then run the same stretch of the (long, straight-line)
+    // per-sample code at the same time and share its instruction fetches.
+    for (u64 k = 0; k < chunk; k++) {
+        __syncthreads();
+        const u64 i = first + k;
+        if (i >= last) continue;
+#else
     for (u64 i = first; i < last; i++) {
+#endif
 #if FT_PREC == 0
         sample64(g, tr, prm, i, A, 0, rec_order, rec_X, rec_R, rec_flags);
 #else
@@ -1748,7 +1790,7 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
 
     accum A;
     A.init(smem + ACC_SMEM_OFFSET);
-    sample_range(g, tr, prm, first, last, A, queue, qcount, qcap, 0, rec_order, rec_X, rec_R, rec_flags);
+    sample_range(g, tr, prm, first, last, chunk, A, queue, qcount, qcap, 0, rec_order, rec_X, rec_R, rec_flags);
     A.finish(acc_out + (size_t)blockIdx.x * ACC_SLOTS);
 }
 
@@ -1866,7 +1908,7 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample_batch(
         skip_lanes(g, threadIdx.x, lanepw, lanebits);
         accum A;
         A.init(smem + ACC_SMEM_OFFSET);
-        sample_range(g, tr, prm, first, last, A, queue, qcount, qcap,
+        sample_range(g, tr, prm, first, last, chunk, A, queue, qcount, qcap,
                      (it << BQ_ITEM_SHIFT) | ((u64)threadIdx.x << BQ_LANE_SHIFT), nullptr, nullptr, nullptr, nullptr);
         A.finish(acc_out + it * ACC_SLOTS);
     }

@@ -13,6 +13,7 @@
 #include "../../include/feyntrop_gb300.h"
 #include "jit.hpp"
 #include "problem.hpp"
+#include "tune.hpp"
 #include "xoshiro.hpp"
 
 namespace ftrt {
@@ -71,10 +72,10 @@ struct ft_plan {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;
-    // launch shape of the sampling kernels (threads per block, minimum resident blocks
-    // per SM given to the register allocator), from a sweep on GB300: the mixed form
-    // gains ~1.6x on deformed integrals from 256 x 2 (168 registers instead of 255)
-    int tuned_block = 256, tuned_minb = 2;
+    // a launch shape under measurement by the autotuner (for one precision)
+    bool forced = false;
+    int forced_prec = 0;
+    ft::launch_shape forced_shape;
 
     ft::kernel_key key(int prec, int record) const
     {
@@ -88,18 +89,14 @@ struct ft_plan {
         k.mode = P.deformed() ? 1 : 0;
         k.only_psi = P.only_psi() ? 1 : 0;
         k.record = record;
-        k.block = tuned_block;
-        k.minb = prec == 0 ? 1 : tuned_minb;
-        if (const char* e = std::getenv("FEYNTROP_GB300_BLOCK")) k.block = std::atoi(e);
-        if (const char* e = std::getenv("FEYNTROP_GB300_MINB")) k.minb = std::atoi(e);
-        // out-of-line FP32 transcendentals pay off where the code is largest (deformed)
-        k.variant = P.deformed() ? 1 : 0;
-        if (const char* e = std::getenv("FEYNTROP_GB300_VARIANT")) k.variant = std::atoi(e);
         k.ek = P.ek;
         k.el = P.el;
         // small tables are staged per block in shared memory; from E = 11 on the table is
         // read through L1 (one cached copy per SM instead of one per block)
         k.table_global = P.E >= 11 ? 1 : 0;
+        // launch shape: a shape being measured by the autotuner, else the tuning table's
+        // (or the default) for this kernel class
+        ft::apply_shape(k, (forced && forced_prec == prec) ? forced_shape : ft::choose_shape(k));
         return k;
     }
 

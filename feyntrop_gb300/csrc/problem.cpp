@@ -154,14 +154,17 @@ struct builder {
     }
 
     // srcs/tropical_sampling.hpp:46-82: |phi/psi + sum m^2 x| summed over probes,
-    // with phi/psi = -trace(L^{-1} PGP) on the contracted graph
+    // with phi/psi = -trace(L^{-1} PGP) on the contracted graph, compared with
+    // 1e-12 pmsqr_ref.  The terms are non-negative and rounded addition is monotone, so
+    // once a partial sum reaches the threshold the full sum does too: the loop stops
+    // there with the same answer (most subgraphs are decided by the first probe).
     bool mass_momentum_spanning(uint64_t sub, int C, const int* cmap, const double* PGP) const
     {
         const int n = C - 1;
-        std::vector<double> L((size_t)n * n), D(n), col(n);
+        double L[64 * 64], D[64], col[64];
         double sum = 0.0;
         for (size_t t = 0; t < X.size(); t++) {
-            std::fill(L.begin(), L.end(), 0.0);
+            std::fill(L, L + (size_t)n * n, 0.0);
             for (int j = 0; j < p.E; j++) {
                 if ((sub >> j) & 1) continue;
                 int k = cmap[p.ek[j]], l = cmap[p.el[j]];
@@ -198,6 +201,7 @@ struct builder {
             for (int j = 0; j < p.E; j++)
                 if (!((sub >> j) & 1)) pxi += p.m2[j] * X[t][j];
             sum += std::fabs(pxi);
+            if (!(sum / pmsqr_ref < 1e-12)) return false;
         }
         return sum / pmsqr_ref < 1e-12;
     }
@@ -406,7 +410,8 @@ prepared prepare(const problem_input& in, int threads)
     const size_t size = 1ULL << E;
     std::vector<structure> st(size);
     if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
-    if (size < 256) threads = 1;
+    // at least 1024 subsets per thread: below that, starting threads costs more than it saves
+    threads = (int)std::max<size_t>(1, std::min<size_t>((size_t)threads, size / 1024));
     {
         std::atomic<size_t> next{0};
         std::exception_ptr err;

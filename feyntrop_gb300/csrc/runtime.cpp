@@ -21,6 +21,8 @@
 #include <stdexcept>
 #include <string>
 #include <vector>
+#include <atomic>
+#include <thread>
 
 #include "../../include/feyntrop_gb300.h"
 #include "jit.hpp"
@@ -447,29 +449,101 @@ const char* ft_last_error(void) { return g_error.c_str(); }
 const char* ft_version(void) { return "feyntrop_gb300 0.1 (sm_103a)"; }
 void ft_free(void* p) { std::free(p); }
 
+// host part of a plan (preprocessing, parameter block, table); threads for the table
+static std::unique_ptr<ft_plan> make_plan(const ft_problem* pb, int threads, int device)
+{
+    ft::problem_input in = input_of(pb);
+    std::unique_ptr<ft_plan> pl(new ft_plan());
+    pl->P = ft::prepare(in, threads);
+    if (pl->P.E > 24) throw std::domain_error("graphs with more than 24 edges are not supported by the GPU sampler");
+    low_rank(pl->P, pl->sigma, pl->q);
+    build_blocks(*pl);
+    pl->device = device;
+    return pl;
+}
+
+// status of a failed plan creation: input errors keep their codes, a missing device
+// (std::logic_error from require_device) is FT_ERR_NO_DEVICE
+static int create_status(const std::exception_ptr& ep)
+{
+    try {
+        std::rethrow_exception(ep);
+    } catch (const std::invalid_argument&) {
+        return status_of(ep);
+    } catch (const std::domain_error&) {
+        return status_of(ep);
+    } catch (const std::logic_error& e) {
+        g_error = e.what();
+        return FT_ERR_NO_DEVICE;
+    } catch (...) {
+        return status_of(ep);
+    }
+}
+
 int ft_plan_create(const ft_problem* pb, ft_plan** out)
 {
     *out = nullptr;
     try {
-        ft::problem_input in = input_of(pb);
-        std::unique_ptr<ft_plan> pl(new ft_plan());
-        pl->P = ft::prepare(in);
-        if (pl->P.E > 24) throw std::domain_error("graphs with more than 24 edges are not supported by the GPU sampler");
+        std::unique_ptr<ft_plan> pl = make_plan(pb, 0, 0);
         require_device();
-        low_rank(pl->P, pl->sigma, pl->q);
-        build_blocks(*pl);
         dev_state();
         cu(cudaGetDevice(&pl->device), "cudaGetDevice");
         *out = pl.release();
         return FT_OK;
-    } catch (const std::logic_error& e) {
-        if (dynamic_cast<const std::invalid_argument*>(&e) || dynamic_cast<const std::domain_error*>(&e))
-            return status_of(std::current_exception());
-        g_error = e.what();
-        return FT_ERR_NO_DEVICE;
     } catch (...) {
-        return status_of(std::current_exception());
+        return create_status(std::current_exception());
     }
+}
+
+int ft_plans_create(const ft_problem* problems, int32_t count, ft_plan** out, int32_t* status)
+{
+    if (!out || (count > 0 && !problems)) {
+        g_error = "ft_plans_create: NULL argument";
+        return FT_ERR_INVALID_ARGUMENT;
+    }
+    for (int i = 0; i < count; i++) {
+        out[i] = nullptr;
+        if (status) status[i] = FT_ERR_RUNTIME;
+    }
+    int device = 0;
+    try {
+        require_device();
+        dev_state();
+        cu(cudaGetDevice(&device), "cudaGetDevice");
+    } catch (...) {
+        const int rc = create_status(std::current_exception());
+        if (status)
+            for (int i = 0; i < count; i++) status[i] = rc;
+        return rc;
+    }
+    // one problem per task on all host threads (each table single-threaded)
+    std::vector<int> rcs(count, FT_OK);
+    std::vector<std::string> msgs(count);
+    std::atomic<int> next{0};
+    auto work = [&]() {
+        for (int i = next.fetch_add(1); i < count; i = next.fetch_add(1)) {
+            try {
+                out[i] = make_plan(&problems[i], 1, device).release();
+            } catch (...) {
+                rcs[i] = create_status(std::current_exception());
+                msgs[i] = g_error;
+            }
+        }
+    };
+    const int nth = (int)std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()), (unsigned)std::max(1, count));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nth; t++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    int first = FT_OK;
+    for (int i = 0; i < count; i++) {
+        if (status) status[i] = rcs[i];
+        if (rcs[i] != FT_OK && first == FT_OK) {
+            first = rcs[i];
+            g_error = "problem " + std::to_string(i) + ": " + msgs[i];
+        }
+    }
+    return first;
 }
 
 void ft_plan_destroy(ft_plan* p) { delete p; }
@@ -654,6 +728,92 @@ int ft_integrate_noalloc(ft_plan* pl, const ft_run_options* o, double* d_slots)
            "finalize");
         return FT_OK;
     } catch (...) {
+        return status_of(std::current_exception());
+    }
+}
+
+int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result* out)
+{
+    try {
+        if (!pl || !out) throw std::invalid_argument("ft_autotune: NULL argument");
+        if (samples < 1000) throw std::invalid_argument("ft_autotune: at least 1000 samples per trial");
+        std::lock_guard<std::mutex> lock(pl->mu);
+        cu(cudaSetDevice(pl->device), "cudaSetDevice");
+        upload(*pl);
+        const int prec = precision == FT_PRECISION_MIXED ? 1 : 0;
+        const bool deformed = pl->P.deformed();
+        // candidates: launch shapes (threads per block x blocks per SM) and code variants
+        std::vector<ft::launch_shape> cands;
+        auto add = [&](int block, int minb, int variant) {
+            ft::launch_shape s;
+            s.block = block;
+            s.minb = minb;
+            s.variant = variant;
+            cands.push_back(s);
+        };
+        if (prec == 1) {
+            const int v = deformed ? 1 : 0;
+            for (int var : {v | 4, v})
+                for (int bm : {512, 256, 128}) add(bm, 512 / bm, var);
+            if (deformed) add(512, 1, 4);
+        } else {
+            const int v = deformed ? 1 : 0;
+            for (int var : {v, v | 4})
+                for (int bm : {256, 128, 512}) add(bm, bm == 128 ? 2 : 1, var);
+        }
+        ft_run_options o{};
+        o.num_samples = samples;
+        o.precision = precision;
+        double best_rate = -1, default_rate = -1;
+        ft::launch_shape best;
+        const ft::launch_shape dflt = ft::default_shape(pl->key(prec, 0));
+        int tried = 0;
+        for (const ft::launch_shape& c : cands) {
+            pl->forced = true;
+            pl->forced_prec = prec;
+            pl->forced_shape = c;
+            double rate = 0;
+            try {
+                ft_run_options w = o;
+                w.num_samples = std::max<uint64_t>(1000, samples / 8);
+                run(*pl, w, pl->stream, nullptr);   // compiles and loads the candidate
+                for (int rep = 0; rep < 2; rep++) {
+                    o.seed = (uint64_t)rep;
+                    run_out ro = run(*pl, o, pl->stream, nullptr);
+                    rate = std::max(rate, (double)samples / (ro.kernel_ms * 1e-3));
+                }
+            } catch (...) {
+                pl->forced = false;
+                throw;
+            }
+            pl->forced = false;
+            tried++;
+            const ft::kernel_key kc = [&] {
+                ft::kernel_key k = pl->key(prec, 0);
+                ft::apply_shape(k, c);
+                return k;
+            }();
+            ft::kernel_key kd = pl->key(prec, 0);
+            ft::apply_shape(kd, dflt);
+            if (kc.block == kd.block && kc.minb == kd.minb && kc.variant == kd.variant)
+                default_rate = std::max(default_rate, rate);
+            if (rate > best_rate) {
+                best_rate = rate;
+                best = c;
+            }
+        }
+        best.rate = best_rate;
+        ft::record_shape(pl->key(prec, 0), best);
+        ft::kernel_key kb = pl->key(prec, 0);
+        out->block = kb.block;
+        out->min_blocks_per_sm = kb.minb;
+        out->variant = kb.variant;
+        out->samples_per_second = best_rate;
+        out->default_samples_per_second = default_rate;
+        out->candidates = tried;
+        return FT_OK;
+    } catch (...) {
+        if (pl) pl->forced = false;
         return status_of(std::current_exception());
     }
 }

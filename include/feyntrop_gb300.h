@@ -57,6 +57,12 @@ typedef struct {
 int ft_plan_create(const ft_problem* problem, ft_plan** out);
 void ft_plan_destroy(ft_plan* plan);
 
+/* ft_plan_create for many problems at once on all host threads (kinematic scans,
+ * batches).  out[i] is NULL where problem i failed; status[i] (may be NULL) holds each
+ * problem's code.  Returns FT_OK, or the code of the first failure (its message, with
+ * the problem's index, in ft_last_error()). */
+int ft_plans_create(const ft_problem* problems, int32_t count, ft_plan** out, int32_t* status);
+
 typedef struct {
     double W;                     /* superficial degree of divergence */
     double IGtr;                  /* tropical normalisation I_G^tr */
@@ -189,6 +195,20 @@ int ft_subgraph_table(const ft_problem* problem, double* Jr, double* r, uint8_t*
  * cache.  *seconds receives the compile time (0 when cached). */
 #define FT_PRECOMPILE_BATCH 0x100
 int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds);
+
+/* Autotuner: times the sampling kernels of this plan's kernel class (topology, eps
+ * orders, regime, precision) under candidate launch shapes (threads per block, blocks
+ * per SM given to the register allocator, code-size variants), `samples` samples per
+ * trial, and records the fastest in the tuning table (in memory and in tuning.json
+ * beside the kernel cache), which every later plan and batch of the class uses.
+ * Compiles each candidate on first use. */
+typedef struct {
+    int32_t block, min_blocks_per_sm, variant;   /* the recorded shape */
+    double samples_per_second;                   /* its rate */
+    double default_samples_per_second;           /* the default shape's rate (-1 if not a candidate) */
+    int32_t candidates;
+} ft_tune_result;
+int ft_autotune(ft_plan* plan, int32_t precision, uint64_t samples, ft_tune_result* out);
 
 /* Measured FP32 and FP64 FMA issue rates of the current device in TFLOP/s (an
  * FMA-chain probe kernel; the denominators of the sampling kernels' roofline). */

@@ -135,3 +135,35 @@ def test_batch_matches_reference_aggregates():
             assert abs(g_dre - dre) <= 1e-6 * dre
     for p in ps:
         p.close()
+
+
+def test_plans_create_matches_single_creation_and_reports_failures():
+    inputs = [PINS["cases"][n]["input"] for n in NAMES]
+    bad = dict(inputs[0], graph=[[[0, 0], 1]] + inputs[0]["graph"][1:])   # a tadpole: invalid argument
+    ps = ft.create_plans(inputs + [bad], skip_failed=True)
+    assert ps[-1] is None
+    for p, x in zip(ps[:-1], inputs):
+        q = ft.Plan(x)
+        assert p.info["IGtr"] == q.info["IGtr"] and p.info["deformed"] == q.info["deformed"]
+        a = p.integrate(100_000, seed=4, precision=ft.MIXED)
+        b = q.integrate(100_000, seed=4, precision=ft.MIXED)
+        assert_same(a, b, ft.MIXED, "create_plans")
+        q.close()
+    with pytest.raises(ft.FeyntropError) as e:
+        ft.create_plans([bad])
+    assert "problem 0" in str(e.value) and "tadpole" in str(e.value)
+    assert e.value.code == ft.FT_ERR_INVALID_ARGUMENT
+
+
+def test_autotune_records_a_shape_and_keeps_the_samples():
+    """The autotuner only changes launch shapes: the same samples give the same counts
+    and the same integral after it recorded its choice."""
+    p = ft.Plan(PINS["cases"]["C1_K4"]["input"])
+    before = p.integrate(300_000, seed=8, precision=ft.MIXED)
+    t = p.autotune(ft.MIXED, samples=1_000_000)
+    assert t["candidates"] >= 4 and t["samples_per_second"] > 0
+    assert t["block"] in (64, 128, 256, 512) and t["variant"] in range(8)
+    assert t["samples_per_second"] >= t["default_samples_per_second"]
+    after = p.integrate(300_000, seed=8, precision=ft.MIXED)
+    assert_same(after, before, ft.MIXED, "after autotune")
+    p.close()

@@ -148,3 +148,16 @@ def test_batch_workloads_are_seeded_and_redraw_rejected_points():
     m, _ = w.mixed_batch(seed=5, counts=(4, 4, 2, 2))
     assert [len(x["graph"]) for x in m] == [3] * 4 + [10] * 4 + [8] * 2 + [8] * 2
     assert [x["lambda"] for x in m[4:8]] == [0, 0.5, 0, 0.5]
+
+
+def test_plans_create_without_a_device_reports_no_device():
+    import ctypes
+    inp = PINS["cases"]["C1_K4"]["input"]
+    a = ft._ProblemArrays(inp)
+    probs = (ft.Problem * 2)(a.struct, a.struct)
+    hs = (ctypes.c_void_p * 2)()
+    st = (ctypes.c_int32 * 2)()
+    rc = ft.lib().ft_plans_create(ctypes.cast(probs, ctypes.c_void_p), 2, ctypes.cast(hs, ctypes.c_void_p),
+                                  ctypes.cast(st, ctypes.c_void_p))
+    assert rc == ft.FT_ERR_NO_DEVICE and list(st) == [ft.FT_ERR_NO_DEVICE] * 2
+    assert hs[0] is None and hs[1] is None
