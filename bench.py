@@ -178,11 +178,13 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
             return False
 
     if args.batched == "scan":
-        inputs, redrawn = workloads.box_pentagon_scan(4096, seed=3, accept=accept)
+        inputs, redrawn = workloads.box_pentagon_scan(args.batch_count or 4096, seed=3, accept=accept)
         name = ("box-pentagon kinematic scan: 4096 points (7 vertices, 8 edges, D=6, 3 eps orders), masses U[0,2], "
                 "invariants U[-10,10], lambda U[0.2,1], N log-uniform [1e5,1e7], Random(3)")
     else:
         inputs, redrawn = workloads.mixed_batch(seed=5, accept=accept)
+        if args.batch_count:
+            inputs = inputs[:args.batch_count]
         name = ("mixed uneven batch: 512 triangles, 512 3-loop ladders, 256 4-loop vacuum wheels, 256 box-pentagons, "
                 "masses U[0,3], N log-uniform [1e5,1e8], Random(5)")
     t0 = time.perf_counter()
@@ -286,6 +288,10 @@ def main():
     ap.add_argument("--batched", default="scan", choices=["scan", "mixed", "none"],
                     help="the batched form's workload (one GPU runs it, rank 0 reports it)")
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--batch-count", type=int, default=0,
+                    help="only the first n integrals of the batch (profiler captures); 0: all")
+    ap.add_argument("--batch-only", action="store_true",
+                    help="only the batched form (profiler captures); prints its object alone")
     ap.add_argument("--batch-fp64-scale", type=float, default=1 / 16)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -308,6 +314,10 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
+    if args.batch_only:
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        print(json.dumps(batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local))), flush=True)
+        return
     N = args.samples
     inp = workloads.double_box(N=N)
     plan = ft.Plan(inp)
@@ -390,11 +400,12 @@ def main():
         e2e_s = t.item()
 
     # merged result over ranks (moments are additive)
+    from feyntrop_gb300 import shard
     moments = r_mixed[-1]["moments"]
     if dist:
         allm = [None] * world
         dist.all_gather_object(allm, moments)
-        moments = [[math.fsum(m[i][k] for m in allm) for k in range(5)] for i in range(len(moments))]
+        moments = shard.merge_moments(allm)
     integral = ft.finalize_moments(moments, plan.K, real_only=not plan.info["deformed"])
 
     if rank != 0:

@@ -439,7 +439,7 @@ int ft_batch_run(ft_batch* b, const ft_run_options* opts, ft_result* results)
                 p->first_item = next;
                 p->nitems = items;
                 next += items;
-                q += (size_t)std::min<unsigned long long>(N, N / 64 + 1024);
+                q += (size_t)std::min<unsigned long long>(N, N / 32 + 1024);
             }
             if (next >= (1ull << 36)) throw std::invalid_argument("ft_batch_run: too many work items");
             g.total_items = next;
