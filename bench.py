@@ -226,6 +226,20 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
                                 "includes": "host preprocessing of every integral, batch creation, one run"}
         b.close()
     out["mixed_over_fp64"] = rates["mixed"] / rates["plain_fp64"]
+    # the CPU path on a bounded, evenly spaced subset of the same integrals
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        pick = list(range(0, len(inputs), max(1, len(inputs) // 8)))[:8]
+        tot_n = tot_t = 0.0
+        kind = None
+        for i in pick:
+            v, n, kind = cpu_rate(inputs[i], args.cpu_seconds / len(pick), threads)
+            tot_n += n
+            tot_t += n / v
+        out["cpu_baseline"] = {"value": tot_n / tot_t, "unit": UNIT, "cores": threads, "kind": kind,
+                               "sample": "integrals %s of the batch, %d samples in total, all host threads"
+                                         % (pick, int(tot_n))}
+        out["mixed_over_cpu"] = rates["mixed"] / out["cpu_baseline"]["value"]
     # per-sample error of the mixed form against the FP64 form on the first 8 integrals
     import numpy as np
     errs = []

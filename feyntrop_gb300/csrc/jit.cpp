@@ -6,6 +6,7 @@
 #include <sys/stat.h>
 
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -24,10 +25,44 @@ unsigned table_smem_bytes(const kernel_key& k)
 {
     // staged table (unless read from global memory), then the per-thread accumulators
     const unsigned entries = 1u << k.E;
-    const unsigned tab = k.table_global ? 0u : (k.prec == 0 ? 25u * entries : 13u * entries);
+    const unsigned tab = k.table_global ? 0u : (k.prec == 0 ? 25u * entries : 17u * entries);
     const unsigned parts = k.mode == 1 ? 4u : 2u;
     const unsigned acc = (unsigned)k.block * parts * (unsigned)k.K * (k.prec == 0 ? 16u : 24u);
     return ((tab + 15u) & ~15u) + acc;
+}
+
+// Tables of the two-float logarithm and exponential of the mixed kernels (FP32 values
+// written exactly as hexadecimal literals):
+//   FT_LOGTAB[3i .. 3i+2] = r_i = fl(1 / (1 + (i + 1/2)/64)), -log(r_i) as hi, lo (i < 64)
+//   FT_EXPTAB[2j .. 2j+1] = 2^(j/32) as hi, lo (j < 32)
+static std::string tables_source()
+{
+    static const std::string text = [] {
+        std::ostringstream s;
+        char buf[64];
+        s << "__device__ const float FT_LOGTAB[192] = {";
+        for (int i = 0; i < 64; i++) {
+            const float r = (float)(1.0 / (1.0 + (i + 0.5) / 64.0));
+            const double nl = -std::log((double)r);
+            const float hi = (float)nl, lo = (float)(nl - (double)hi);
+            for (float v : {r, hi, lo}) {
+                std::snprintf(buf, sizeof buf, "%af,", (double)v);
+                s << buf;
+            }
+        }
+        s << "};\n__device__ const float FT_EXPTAB[64] = {";
+        for (int j = 0; j < 32; j++) {
+            const double t = std::exp2(j / 32.0);
+            const float hi = (float)t, lo = (float)(t - (double)hi);
+            for (float v : {hi, lo}) {
+                std::snprintf(buf, sizeof buf, "%af,", (double)v);
+                s << buf;
+            }
+        }
+        s << "};\n";
+        return s.str();
+    }();
+    return text;
 }
 
 std::string kernel_source(const kernel_key& k)
@@ -46,6 +81,7 @@ std::string kernel_source(const kernel_key& k)
     s << "};\n__device__ constexpr int FT_EL[" << k.E << "] = {";
     for (int e = 0; e < k.E; e++) s << (e ? "," : "") << k.el[e];
     s << "};\n";
+    s << tables_source();
     s << ft_sample_body_source;
     return s.str();
 }

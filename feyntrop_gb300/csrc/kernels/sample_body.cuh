@@ -109,7 +109,8 @@ static __device__ FT_MATHFN void m_sincos(float x, float* s, float* c) { sincosf
 // prm + P_SIZE + (P_SIZE + 1) / 2 (the mixed form reads only those two)
 
 // ------------------------------------------------------------------ table layout
-// [w64 | Jr64 | rinv64 : 8 bytes each][meta : 1 byte][pad to 16][w32 | Jr32 | rinv32]
+// [w64 | Jr64 | rinv64 : 8 bytes each][meta : 1 byte][pad to 16][w32 | Jr32 : 4 bytes each]
+// [rinv32 : (hi, lo) float pairs]
 #define T_ENTRIES (1u << FT_E)
 #define T_W64 0
 #define T_JR64 (8u * T_ENTRIES)
@@ -118,7 +119,7 @@ static __device__ FT_MATHFN void m_sincos(float x, float* s, float* c) { sincosf
 #define T_F32 ((25u * T_ENTRIES + 15u) & ~15u)
 #define T_W32 (T_F32)
 #define T_JR32 (T_F32 + 4u * T_ENTRIES)
-#define T_RI32 (T_F32 + 8u * T_ENTRIES)
+#define T_RI32 (T_F32 + 8u * T_ENTRIES)   // (hi, lo) float pairs: 1/r in two-float
 
 // ------------------------------------------------------------------ accumulator slots
 // per eps order j: [8j + 0..7] = re S1 (hi, lo), re S2 (hi, lo), im S1 (hi, lo), im S2 (hi, lo)
@@ -472,7 +473,7 @@ static __device__ __forceinline__ f2 f2_add2(f2 a, f2 b)
     return f2_add(r, b.lo);
 }
 
-// log(1 - u) for u = (x >> 11) 2^-53, to about 1e-7 absolute, with integer and FP32
+// log(1 - u) for u = (x >> 11) 2^-53, to about 1e-7 absolute (undeformed integrands), with integer and FP32
 // instructions only (64-bit integer to float conversions would run on the FP64 pipe).
 // A positive integer v is turned into the float bits of 2^k (1 + f) directly: k from
 // the leading-zero count, f from the next 23 bits rounded (a carry bumps k).
@@ -483,7 +484,7 @@ static __device__ __forceinline__ int float_bits_of(u64 v, int scale_exp)
     return ((63 - lz + scale_exp + 127) << 23) + (int)frac;
 }
 
-static __device__ __forceinline__ f2 log1m_u(u64 x)
+static __device__ __forceinline__ f2 log1m_u32(u64 x)
 {
     const u64 m = x >> 11;
     f2 r;
@@ -504,6 +505,82 @@ static __device__ __forceinline__ f2 log1m_u(u64 x)
     a.hi = kk * LN2_HI;
     a.lo = kk * LN2_LO;
     return f2_add(a, m_log1p(f));
+}
+
+static __device__ __forceinline__ f2 f2_two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    f2 r;
+    r.hi = s;
+    r.lo = (a - (s - bb)) + (b - bb);
+    return r;
+}
+
+// log(1 - u) for u = (x >> 11) 2^-53 in two-float, to about 1e-12 absolute, with integer
+// and FP32 instructions only (64-bit conversions and FP64 would run on the FP64 pipe).
+// Table-driven reduction after Tang (ACM TOMS 16, 1990): 1 - u = q 2^-53 with the
+// integer q = 2^53 - (x >> 11) exactly, q = 2^k M with M in [1, 2) held as two floats
+// (47 fraction bits); c_i = 1 + (i + 1/2)/64 for the top 6 fraction bits i,
+// r_i = fl(1/c_i) and -log r_i (two-float) from FT_LOGTAB; z = M r_i - 1 (|z| < 1/100)
+// from exact products, log M = -log r_i + log1p(z) with log1p(z) = z - z^2/2 + z^3/3 -
+// z^4/4 + z^5/5, the terms past z in FP32.
+static __device__ __forceinline__ f2 log1m_u2(u64 x)
+{
+    const u64 q = (1ull << 53) - (x >> 11);   // 1 .. 2^53
+    const int lz = __clzll(q);
+    const u64 mb = q << lz;                    // M = mb / 2^63, leading 1 at bit 63
+    const u32 top = (u32)(mb >> 40);           // 1 + 23 fraction bits
+    const float m_hi = __int_as_float(0x3f800000 | (int)(top & 0x7fffffu));
+    const float m_lo = (float)(u32)((mb >> 16) & 0xffffffull) * 0x1.0p-47f;
+    const int i = (int)((top >> 17) & 63u);
+    const float r = FT_LOGTAB[3 * i], nl_hi = FT_LOGTAB[3 * i + 1], nl_lo = FT_LOGTAB[3 * i + 2];
+    // z = M r - 1: m_hi r = p + e exactly, p - 1 exact (p within 1% of 1)
+    const float p = m_hi * r;
+    const float e = fmaf(m_hi, r, -p);
+    const f2 z = f2_two_sum(p - 1.0f, fmaf(m_lo, r, e));
+    const float zh = z.hi;
+    const float tail = zh * zh * fmaf(zh, fmaf(zh, fmaf(zh, 0.2f, -0.25f), 0.333333343f), -0.5f);
+    // (k - 53) ln2 with ln2 in three parts (LN2_HI has 16 bits: the products are exact)
+    const float kk = (float)(10 - lz);          // k - 53 with k = 63 - lz
+    const float LN2_HI = 0.693145751953125f, LN2_LO = 1.428606765330187e-06f, LN2_LO2 = 5.497923e-14f;
+    f2 acc = f2_two_sum(kk * LN2_HI, nl_hi);
+    acc = f2_add(acc, fmaf(kk, LN2_LO, nl_lo));
+    acc = f2_add(acc, fmaf(kk, LN2_LO2, z.lo + tail));
+    return f2_add(acc, zh);
+}
+
+// e^a for a two-float a (|a| < 80) in two-float, about 1e-12 relative; table-driven
+// after Tang (ACM TOMS 15, 1989): a = (32 m + j) ln2/32 + s with |s| <= ln2/64,
+// e^a = 2^m 2^(j/32) e^s, 2^(j/32) as two floats from FT_EXPTAB, e^s = 1 + s + s^2/2 +
+// s^3/6 + s^4/24 with the terms past s in FP32.  ln2/32 = C1 + C2 + C3, C1 with 11
+// significant bits so that k C1 is exact for |k| < 2^13.
+static __device__ __forceinline__ f2 exp_f2(f2 a)
+{
+    const float C1 = 0x1.62cp-6f, C2 = 0x1.217f7ep-17f, C3 = -0x1.c610cap-42f;
+    const float kf = rintf(a.hi * 46.1662407f);
+    const int k = (int)kf;
+    // a - k C1 is exact; k C2 = p2 + e2 exactly
+    const float p2 = kf * C2;
+    const float e2 = fmaf(kf, C2, -p2);
+    f2 sv = f2_two_sum(fmaf(-kf, C1, a.hi), -p2);
+    sv = f2_add(sv, fmaf(-kf, C3, a.lo - e2));
+    const float sh = sv.hi;
+    const float tail = sh * sh * fmaf(sh, fmaf(sh, 0.0416666679f, 0.166666672f), 0.5f);
+    // e^s = 1 + es
+    f2 es = f2_two_sum(sh, sv.lo + tail);
+    es = f2_add(f2_two_sum(1.0f, es.hi), es.lo);
+    const int j = k & 31, m = k >> 5;
+    const float t_hi = FT_EXPTAB[2 * j], t_lo = FT_EXPTAB[2 * j + 1];
+    // (t_hi + t_lo)(es.hi + es.lo) with the product error of the leading term
+    const float ph = t_hi * es.hi;
+    const float pl = fmaf(t_hi, es.hi, -ph) + fmaf(t_hi, es.lo, t_lo * es.hi);
+    const f2 pr = f2_two_sum(ph, pl);
+    const float sc = __int_as_float((127 + m) << 23);   // 2^m, |m| < 126
+    f2 out;
+    out.hi = pr.hi * sc;
+    out.lo = pr.lo * sc;
+    return out;
 }
 
 // The reference's comparison, exactly (FP64, ascending edges, first running sum above
@@ -570,7 +647,7 @@ static __device__ __forceinline__ int draw_sector32(xo& g, const table_ref& t, c
         }
         sub ^= 1u << cut;
         JJr = Jr[sub];
-        const float rinv = ri[sub];
+        const float2 rinv = ((const float2*)ri)[sub];   // 1/r as two floats
         const unsigned m = meta[sub];
         const bool mm = (m >> 7) != 0;
         const int L = (int)(m & 127u);
@@ -585,10 +662,16 @@ static __device__ __forceinline__ int draw_sector32(xo& g, const table_ref& t, c
         }
         if (FT_RECORD) ord[j] = (unsigned char)cut;
         if (j < FT_E - 1) {
-            f2 l = log1m_u(g.next());
-            // (hi + lo) * rinv with the product error kept
-            float p = l.hi * rinv;
-            float pe = fmaf(l.hi, rinv, -p) + l.lo * rinv;
+#if FT_MODE == 1
+            // deformed integrands: the phase moves by |theta| per unit of log X, so the
+            // sector point is carried to ~1e-12 (two-float logarithm)
+            f2 l = log1m_u2(g.next());
+#else
+            f2 l = log1m_u32(g.next());
+#endif
+            // (hi + lo) * (rinv.x + rinv.y) with the product error kept
+            float p = l.hi * rinv.x;
+            float pe = fmaf(l.hi, rinv.x, -p) + fmaf(l.hi, rinv.y, l.lo * rinv.x);
             f2 inc;
             inc.hi = p;
             inc.lo = pe;
@@ -856,6 +939,13 @@ static __device__ FT_DFFN df df_inv(df x)
     return df_add(df_mk(r), df_mul(df_mk(r), e));
 }
 static __device__ __forceinline__ float df_f(df x) { return x.hi + x.lo; }
+static __device__ __forceinline__ df df_of(f2 x)
+{
+    df r;
+    r.hi = x.hi;
+    r.lo = x.lo;
+    return r;
+}
 
 // x-derivatives of phi/psi at the sample point (srcs/laplacian.hpp:102-215) and the
 // deformation angle theta = -lambda (d(phi/psi)/dx + m^2) (srcs/feynman_integral.hpp:290-291).
@@ -865,7 +955,7 @@ static __device__ __forceinline__ float df_f(df x) { return x.hi + x.lo; }
 // potentials h_r = G q_r and their drops across the edges, the effective-resistance
 // combinations t, and the Minkowski products s.  Outputs theta and the upper
 // triangle of H in FP32.  pd: the parameter block as two-float pairs.
-static __device__ __forceinline__ void derivatives_df(const float* Xi32, const float* pd, df* theta_out,
+static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f2* XiT, const float* pd, df* theta_out,
                                                       float (*H_out)[FT_E])
 {
     df c[FT_N][FT_N], g[FT_N];
@@ -879,9 +969,9 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
     for (int e = 0; e < FT_E; e++) {
         const int k = FT_EK[e], l = FT_EL[e];
         if (k == FT_V - 1)
-            g[l] = df_add(g[l], df_mk(Xi32[e]));
+            g[l] = df_add(g[l], df_of(XiT[e]));
         else
-            c[l][k] = df_add(c[l][k], df_mk(Xi32[e]));
+            c[l][k] = df_add(c[l][k], df_of(XiT[e]));
     }
     df a[FT_N][FT_N], id[FT_N];
 #pragma unroll
@@ -963,7 +1053,7 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
             s = df_fma(sig_hb[r], hb[r][a2], s);
         }
         const df t = df_sub(df_add(Gx(ka, ka), Gx(la, la)), df_add(Gx(ka, la), Gx(ka, la)));
-        const df xi = df_mk(Xi32[a2]);
+        const df xi = df_of(XiT[a2]);
         const df xa = df_mul(xi, xi);
         const df xas = df_mul(xa, s);
         df m2;
@@ -1102,6 +1192,24 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     for (int e = 0; e < FT_E; e++) lmin = fminf(lmin, lx[e].hi);
     const float sh = rintf(0.5f * lmin);
     float X[FT_E], Xi[FT_E];
+#if FT_MODE == 1
+    // 1/X in two-float for the derivative block (theta is a function of X whose phase
+    // effect grows with |theta|); X and 1/X in FP32 from it
+    f2 Xi2[FT_E];
+    bool xbad = false;
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        const f2 a = f2_add(lx[e], -sh);
+        Xi2[e] = exp_f2(f2_make(-a.hi, -a.lo));
+        Xi[e] = Xi2[e].hi;
+        X[e] = rcp_(Xi[e]);
+        xbad |= !(Xi[e] > 1e-30f && Xi[e] < 1e30f);
+    }
+    if (xbad) {   // outside the two-float exponential's range: the FP64 pass takes it
+        need64 = true;
+        return false;
+    }
+#else
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
         const f2 a = f2_add(lx[e], -sh);
@@ -1109,6 +1217,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
         X[e] = fmaf(ep, a.lo, ep);
         Xi[e] = fmaf(em, -a.lo, em);
     }
+#endif
     const f2 lFs = f2_add(lF, -(float)FT_LOOPS * sh);   // log psi_tr in the frame
     const f2 lGs = f2_add(lG, -sh);                      // log V_tr = log(xi_tr / psi_tr)
     elim<float, float> L;
@@ -1176,7 +1285,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     // which cancel in FP32 for a sizeable fraction of sectors; this block runs in FP64.
     df theta[FT_E];
     float H[FT_E][FT_E];
-    derivatives_df(Xi, pd, theta, H);
+    derivatives_df(Xi, Xi2, pd, theta, H);
     cx<float> cX[FT_E], cy[FT_E];
     // phase sums in two-float: sum theta and nu . theta
     f2 xnu = f2_make(0.0f, 0.0f), thsum = f2_make(0.0f, 0.0f);
@@ -1445,7 +1554,7 @@ static __device__ __forceinline__ void skip_lanes(xo& g, u32 lane, const u64* __
 #elif FT_PREC == 0
 #define SM_USED (25u * T_ENTRIES)
 #else
-#define SM_USED (13u * T_ENTRIES)
+#define SM_USED (17u * T_ENTRIES)
 #endif
 static __device__ __forceinline__ void copy_bytes(unsigned char* dst, const unsigned char* __restrict__ src, u32 bytes)
 {
@@ -1480,12 +1589,12 @@ static __device__ __forceinline__ table_ref stage_table(unsigned char* sm, const
     t.ri = sm + T_RI64;
     t.meta = sm + T_META;
 #else
-    copy_bytes(sm, tab + T_F32, 12u * T_ENTRIES);
-    copy_bytes(sm + 12u * T_ENTRIES, tab + T_META, T_ENTRIES);
+    copy_bytes(sm, tab + T_F32, 16u * T_ENTRIES);
+    copy_bytes(sm + 16u * T_ENTRIES, tab + T_META, T_ENTRIES);
     t.w = sm;
     t.Jr = sm + 4u * T_ENTRIES;
     t.ri = sm + 8u * T_ENTRIES;
-    t.meta = sm + 12u * T_ENTRIES;
+    t.meta = sm + 16u * T_ENTRIES;
 #endif
     __syncthreads();
     return t;

@@ -190,7 +190,7 @@ void build_blocks(ft_plan& pl)
     }
     const size_t N = 1ULL << E;
     const size_t f32 = (25 * N + 15) & ~(size_t)15;
-    pl.tab.assign(f32 + 12 * N, 0);
+    pl.tab.assign(f32 + 16 * N, 0);
     double* w64 = (double*)pl.tab.data();
     double* Jr64 = w64 + N;
     double* ri64 = w64 + 2 * N;
@@ -206,7 +206,8 @@ void build_blocks(ft_plan& pl)
         meta[s] = (unsigned char)((p.mm[s] ? 0x80 : 0) | (p.L[s] & 0x7f));
         w32[s] = (float)w64[s];
         Jr32[s] = (float)Jr64[s];
-        ri32[s] = (float)ri64[s];
+        ri32[2 * s] = (float)ri64[s];   // 1/r as two floats (hi, lo)
+        ri32[2 * s + 1] = (float)(ri64[s] - (double)ri32[2 * s]);
     }
 }
 
