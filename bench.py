@@ -441,6 +441,19 @@ def main():
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": "%d samples of the double-box workload (same stream), all host threads" % nsample}
     traffic = dram_traffic("ft_sample mixed double_box")
+    # per-launch duration of the sampling kernels (events inside ft_integrate around
+    # ft_sample and its FP64 pass, on the integration stream)
+    kms = sum(r["kernel_ms"] for r in r_mixed) / len(r_mixed)
+    achieved = flops * N / (kms * 1e-3) / 1e12
+    hbm = None
+    try:
+        peaks = json.load(open(os.path.join(HERE, "MEASURED_PEAKS.json")))
+        if traffic:
+            gbs = traffic / (kms * 1e-3) / 1e9
+            hbm = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
+                   "peak_source": "measured (MEASURED_PEAKS.json)"}
+    except (OSError, ValueError, KeyError):
+        pass
     batched = None
     if args.batched != "none" and rank == 0:
         batched = batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local))
@@ -463,10 +476,13 @@ def main():
         "integral": integral,
         "time_to_target_sigma_s": {"target": "1e-4 * |Re I0|", "mixed": (sigma1 / target) ** 2 / value,
                                    "fp64": (sigma1 / target) ** 2 / value64},
-        "roofline": {"bound": "fp32", "achieved": flops * value / world / 1e12, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": flops * value / world / 1e12 / fp32_peak, "traffic": traffic,
-                     "note": "algorithmic flops per sample %.0f (reference algorithm); peak = FP32 FMA issue "
-                             "rate measured live by an FMA-chain probe (FP64: %.2f TFLOP/s)" % (flops, fp64_peak)},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
+                     "hbm": hbm,
+                     "note": "algorithmic flops per sample %.0f (reference algorithm) x samples per launch / the "
+                             "sampling kernels' CUDA-event time (ft_sample + its FP64 pass, %.2f ms); peak = FP32 "
+                             "FMA issue rate measured live by an FMA-chain probe (FP64: %.2f TFLOP/s). Neither "
+                             "HBM nor tensor cores bound this path: see hbm" % (flops, kms, fp64_peak)},
         "e2e": {"value": N * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks,
