@@ -13,6 +13,7 @@ py_feyntrop (the reference's Python front end) is mirrored in
 feyntrop_gb300.py_feyntrop.
 """
 import ctypes
+import math
 import json
 import os
 import threading
@@ -325,6 +326,44 @@ class Batch:
         for i, r in enumerate(ras):
             r.res = res[i]
             out.append(r.as_dict(self.plans[i].info["IGtr"]))
+        return out
+
+    def run_to_accuracy(self, rel_target, pilot=100_000, max_samples=10**10, seeds=0, eps_order=0, stream=None):
+        """Variance-adaptive sample counts: a pilot run of `pilot` samples per integral
+        estimates each integral's per-sample spread; a second run continues every
+        integral's stream (first sample = pilot) with the samples that bring its
+        standard error at eps order `eps_order` to rel_target times |value| (at most
+        max_samples in total). The moments of both runs are merged, so each result is
+        that of one run over all its samples. Returns the result dicts, each with
+        "samples" (the total used)."""
+        from . import shard
+        n = len(self.plans)
+        first = self.run(pilot, seeds=seeds, stream=stream)
+        extra = []
+        for r in first:
+            (re, dre), (im, dim) = r["integral"][eps_order]
+            scale = max(abs(re), abs(im))
+            spread = max(dre, dim) * math.sqrt(pilot)       # per-sample standard deviation
+            if scale == 0 or not math.isfinite(spread):
+                need = pilot
+            else:
+                need = (spread / (rel_target * scale)) ** 2
+            extra.append(int(min(max_samples, max(pilot, math.ceil(need)))) - pilot)
+        out = []
+        if any(e > 0 for e in extra):
+            second = self.run([max(e, 1) for e in extra], seeds=seeds, first_samples=pilot, stream=stream)
+        else:
+            second = [None] * n
+        for i, (a, b, e) in enumerate(zip(first, second, extra)):
+            moments = a["moments"] if e <= 0 else shard.merge_moments([a["moments"], b["moments"]])
+            res = dict(a if e <= 0 else b)
+            res["moments"] = moments
+            res["integral"] = finalize_moments(moments, self.plans[i].K, not self.plans[i].info["deformed"])
+            res["samples"] = pilot + max(e, 0)
+            if e > 0:
+                for k in ("kept", "dropped", "fp64_fallback", "exact_steps", "robust"):
+                    res[k] = a[k] + b[k]
+            out.append(res)
         return out
 
     def info(self):

@@ -167,3 +167,18 @@ def test_autotune_records_a_shape_and_keeps_the_samples():
     after = p.integrate(300_000, seed=8, precision=ft.MIXED)
     assert_same(after, before, ft.MIXED, "after autotune")
     p.close()
+
+
+def test_run_to_accuracy_reaches_the_target_on_the_same_samples(plans):
+    """Variance-adaptive N: every integral ends at (about) the requested relative error,
+    and the merged pilot + continuation equals one run over the same samples."""
+    b = ft.Batch(plans, ft.MIXED)
+    out = b.run_to_accuracy(0.02, pilot=20_000, max_samples=5_000_000, seeds=3)
+    for i, r in enumerate(out):
+        (re, dre), (im, dim) = r["integral"][0]
+        scale = max(abs(re), abs(im))
+        if r["samples"] < 5_000_000:
+            assert max(dre, dim) <= 0.03 * scale, (NAMES[i], r["samples"], re, dre, im, dim)
+        single = plans[i].integrate(r["samples"], seed=3, precision=ft.MIXED)
+        assert_same(r, single, ft.MIXED, NAMES[i])
+    b.close()
