@@ -930,7 +930,18 @@ static __device__ FT_DFFN df df_mul(df x, df y)
     e = fmaf(x.lo, y.hi, e);
     return df_norm(p, e);
 }
-static __device__ __forceinline__ df df_fma(df x, df y, df z) { return df_add(df_mul(x, y), z); }
+// x y + z: the leading product exact (FMA residual), one two-sum with z.hi, the small
+// terms added once
+static __device__ FT_DFFN df df_fma(df x, df y, df z)
+{
+    const float p = x.hi * y.hi;
+    const float pe = fmaf(x.hi, y.hi, -p);
+    const float s = p + z.hi;
+    const float bb = s - p;
+    float e = (p - (s - bb)) + (z.hi - bb);
+    e += pe + fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, z.lo));
+    return df_norm(s, e);
+}
 static __device__ FT_DFFN df df_inv(df x)
 {
     // one Newton step from the FP32 reciprocal: r + r (1 - x r)
