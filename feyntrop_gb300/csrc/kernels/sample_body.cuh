@@ -944,10 +944,11 @@ static __device__ FT_DFFN df df_fma(df x, df y, df z)
 }
 static __device__ FT_DFFN df df_inv(df x)
 {
-    // one Newton step from the FP32 reciprocal: r + r (1 - x r)
+    // one Newton step from the FP32 reciprocal r: 1/x = r (1 + e) with e = 1 - x r;
+    // 1 - x.hi r (about 2^-23) is exact to 2^-47 by the FMA, then x.lo r is removed
     const float r = rcp_(x.hi);
-    const df e = df_sub(df_mk(1.0f), df_mul(x, df_mk(r)));
-    return df_add(df_mk(r), df_mul(df_mk(r), e));
+    const float e = fmaf(-x.lo, r, fmaf(-x.hi, r, 1.0f));
+    return df_norm(r, r * e);
 }
 static __device__ __forceinline__ float df_f(df x) { return x.hi + x.lo; }
 static __device__ __forceinline__ df df_of(f2 x)
