@@ -83,7 +83,8 @@ class Result(ctypes.Structure):
 class TuneResult(ctypes.Structure):
     _fields_ = [("block", ctypes.c_int32), ("min_blocks_per_sm", ctypes.c_int32), ("variant", ctypes.c_int32),
                 ("samples_per_second", ctypes.c_double), ("default_samples_per_second", ctypes.c_double),
-                ("candidates", ctypes.c_int32)]
+                ("candidates", ctypes.c_int32), ("batch_chunk", ctypes.c_uint64),
+                ("batch_samples_per_second", ctypes.c_double)]
 
 
 class BatchInfo(ctypes.Structure):

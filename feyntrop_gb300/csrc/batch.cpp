@@ -202,7 +202,9 @@ void build(ft_batch& b)
             g.k64 = &ft::get_kernels(k64);
         }
         const ft::launch_shape tuned = ft::choose_shape(g.key);
-        g.chunk = env_u64("FEYNTROP_GB300_BATCH_CHUNK", tuned.chunk ? tuned.chunk : (prec ? 128 : 16));
+        g.chunk = ft::chunk_override()
+                      ? ft::chunk_override()
+                      : env_u64("FEYNTROP_GB300_BATCH_CHUNK", tuned.chunk ? tuned.chunk : (prec ? 128 : 16));
         if (g.chunk < 1 || g.chunk >= (1ull << 18)) throw std::invalid_argument("batch chunk out of range");
         g.lanebits = 1;
         while ((1 << g.lanebits) < g.ks->block) g.lanebits++;

@@ -805,6 +805,44 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
         }
         best.rate = best_rate;
         ft::record_shape(pl->key(prec, 0), best);
+        // the batch work item (samples per thread) of the class, under the chosen shape:
+        // a batch of this one integral per candidate
+        double best_batch = -1;
+        unsigned long long best_chunk = 0;
+        for (unsigned long long c : {32ull, 64ull, 128ull, 256ull}) {
+            ft::set_chunk_override(c);
+            ft_batch* b = nullptr;
+            int rc = ft_batch_create(&pl, 1, prec, &b);
+            ft::set_chunk_override(0);
+            if (rc != FT_OK) throw std::runtime_error(std::string("ft_autotune: batch: ") + g_error);
+            std::vector<double> avg(4 * pl->P.K);
+            ft_result r{};
+            r.num_eps_terms = pl->P.K;
+            r.re_avg = avg.data();
+            r.re_acc = avg.data() + pl->P.K;
+            r.im_avg = avg.data() + 2 * pl->P.K;
+            r.im_acc = avg.data() + 3 * pl->P.K;
+            double rate = 0;
+            for (int rep = 0; rep < 3 && rc == FT_OK; rep++) {
+                ft_run_options bo = o;
+                bo.seed = (uint64_t)rep;
+                bo.stream = nullptr;
+                rc = ft_batch_run(b, &bo, &r);
+                ft_batch_info bi{};
+                ft_batch_get_info(b, &bi);
+                if (rep > 0 && bi.kernel_ms > 0) rate = std::max(rate, (double)samples / (bi.kernel_ms * 1e-3));
+            }
+            ft_batch_destroy(b);
+            if (rc != FT_OK) throw std::runtime_error(std::string("ft_autotune: batch run: ") + g_error);
+            if (rate > best_batch) {
+                best_batch = rate;
+                best_chunk = c;
+            }
+        }
+        best.chunk = best_chunk;
+        ft::record_shape(pl->key(prec, 0), best);
+        out->batch_chunk = best_chunk;
+        out->batch_samples_per_second = best_batch;
         ft::kernel_key kb = pl->key(prec, 0);
         out->block = kb.block;
         out->min_blocks_per_sm = kb.minb;

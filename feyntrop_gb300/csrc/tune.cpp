@@ -134,6 +134,10 @@ void record_shape(const kernel_key& k, const launch_shape& s)
     save_locked();
 }
 
+static thread_local unsigned long long t_chunk_override = 0;
+void set_chunk_override(unsigned long long chunk) { t_chunk_override = chunk; }
+unsigned long long chunk_override() { return t_chunk_override; }
+
 void clear_shapes()
 {
     std::lock_guard<std::mutex> lock(g_mu);

@@ -36,4 +36,9 @@ void clear_shapes();
 // applies shape s to k and shrinks the block until its shared memory fits
 void apply_shape(kernel_key& k, const launch_shape& s);
 
+// batch work-item size forced on batches created by this thread (0: none); the
+// autotuner sets it while it measures candidates
+void set_chunk_override(unsigned long long chunk);
+unsigned long long chunk_override();
+
 }  // namespace ft

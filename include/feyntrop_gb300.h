@@ -199,7 +199,8 @@ int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds)
 /* Autotuner: times the sampling kernels of this plan's kernel class (topology, eps
  * orders, regime, precision) under candidate launch shapes (threads per block, blocks
  * per SM given to the register allocator, code-size variants), `samples` samples per
- * trial, and records the fastest in the tuning table (in memory and in tuning.json
+ * trial, then the batch work-item size (samples per thread: 32 .. 256) under the chosen
+ * shape, and records both in the tuning table (in memory and in tuning.json
  * beside the kernel cache), which every later plan and batch of the class uses.
  * Compiles each candidate on first use. */
 typedef struct {
@@ -207,6 +208,8 @@ typedef struct {
     double samples_per_second;                   /* its rate */
     double default_samples_per_second;           /* the default shape's rate (-1 if not a candidate) */
     int32_t candidates;
+    uint64_t batch_chunk;                        /* recorded batch work item: samples per thread */
+    double batch_samples_per_second;             /* its rate in a batch of this integral */
 } ft_tune_result;
 int ft_autotune(ft_plan* plan, int32_t precision, uint64_t samples, ft_tune_result* out);
 
