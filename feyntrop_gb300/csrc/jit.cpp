@@ -255,6 +255,7 @@ const kernel_set& get_kernels(const kernel_key& key)
     cudaFree(0);   // make the runtime's primary context current for the driver calls
     kernel_set ks;
     ks.block = key.block;
+    ks.variant = key.variant;
     const std::string cubin = cubin_for(key, &ks.compile_seconds);
     check(drv().ModuleLoadData(&ks.module, cubin.data()), "cuModuleLoadData");
     const char* sname = key.batch ? "ft_sample_batch" : "ft_sample";

@@ -33,6 +33,7 @@ struct kernel_set {
     CUfunction sample = nullptr;   // ft_sample (ft_sample_batch in batch modules)
     CUfunction queue = nullptr;    // ft_sample_queue / ft_sample_queue_batch (FP64 modules only)
     int block = 128;
+    int variant = 0;               // FT_VARIANT of the module
     unsigned smem = 0;             // dynamic shared memory per block
     int regs = 0;
     int local_bytes = 0;

@@ -263,9 +263,27 @@ struct launch_geometry {
     int lanebits;
 };
 
-launch_geometry geometry(const ft::kernel_set& ks, unsigned long long N)
+// Threads of a launch and samples per thread.  Kernels without the per-sample block
+// barrier (the FP64 form) get at most 128 samples per thread, in whole waves of resident
+// blocks (a multiple of the SM count): with long static chunks the warps of a block
+// drift apart and the block waits at its final reduction for its slowest warp (the
+// 5-loop cube ran 6x slower at 2570 samples per thread than at 128).  Kernels with the
+// barrier keep their warps together and run one wave of long chunks (more waves cost
+// them 1-2 % per halving of the chunk).  waves = false: one wave (the no-allocation
+// path, whose scratch holds a bounded number of blocks).
+launch_geometry geometry(const ft::kernel_set& ks, unsigned long long N, bool waves = true)
 {
-    const unsigned long long max_threads = (unsigned long long)dev_state().sms * ks.blocks_per_sm * ks.block;
+    const unsigned long long per_wave = (unsigned long long)dev_state().sms * ks.blocks_per_sm * ks.block;
+    unsigned long long w = 1;
+    if (waves && N > 0 && !(ks.variant & 4)) {
+        static const unsigned long long cap = [] {
+            const char* e = std::getenv("FEYNTROP_GB300_CHUNK_CAP");
+            const unsigned long long v = e ? std::strtoull(e, nullptr, 10) : 128ull;
+            return v ? v : 128ull;
+        }();
+        w = std::max(1ull, (N + per_wave * cap - 1) / (per_wave * cap));
+    }
+    const unsigned long long max_threads = per_wave * w;
     launch_geometry g;
     g.chunk = N == 0 ? 1 : (N + max_threads - 1) / max_threads;
     const unsigned long long threads = N == 0 ? 1 : (N + g.chunk - 1) / g.chunk;
@@ -686,7 +704,7 @@ int ft_integrate_noalloc(ft_plan* pl, const ft_run_options* o, double* d_slots)
                 "precision first (loading them allocates)");
         const unsigned long long N = o->num_samples;
         if (N == 0) throw std::invalid_argument("ft_integrate_noalloc: num_samples must be positive");
-        const launch_geometry g = geometry(*ks, N);
+        const launch_geometry g = geometry(*ks, N, false);
         const unsigned qblocks = prec ? (unsigned)(dev_state().sms * std::max(1, k64->queue_blocks_per_sm)) : 0;
         if (g.blocks + qblocks > NOALLOC_MAX_BLOCKS || g.lanebits > NOALLOC_MAX_LANE_BITS)
             throw std::invalid_argument("ft_integrate_noalloc: launch exceeds the static scratch (2048 blocks)");
@@ -759,7 +777,7 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
             if (deformed) add(512, 1, 4);
         } else {
             const int v = deformed ? 1 : 0;
-            for (int var : {v, v | 4})
+            for (int var : {v | 4, v})
                 for (int bm : {256, 128, 512}) add(bm, bm == 128 ? 2 : 1, var);
         }
         ft_run_options o{};
