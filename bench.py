@@ -259,6 +259,41 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
     return out
 
 
+def configs_section(args, ft, workloads, torch, flush):
+    """The other single-integral configurations, each timed like the headline step
+    (one warm-up, two timed integrations with CUDA events on the integration stream,
+    L2 flushed between them), mixed and plain FP64:
+      K4:   complete graph K4, Euclidean, masses 0..5, 3 eps orders, N = 1e7;
+      cube: 5-loop 2-point cube graph (8 vertices, 12 edges), Euclidean, 4 eps orders,
+            N = 1e9 mixed (plain FP64 on 1e8 of the same stream: the rate does not
+            depend on N at these sizes)."""
+    stream = torch.cuda.Stream()
+    out = {}
+    for name, inp, n_mixed, n_fp64 in (("K4", workloads.k4_euclidean(), 10 ** 7, 10 ** 7),
+                                      ("cube", workloads.cube_propagator(), 10 ** 9, 10 ** 8)):
+        plan = ft.Plan(inp)
+        entry = {"workload": name, "samples_mixed": n_mixed, "samples_fp64": n_fp64}
+        for prec, n, tag in ((ft.MIXED, n_mixed, "mixed"), (ft.FP64, n_fp64, "plain_fp64")):
+            times, res = [], None
+            with torch.cuda.stream(stream):
+                for step in range(3):
+                    flush.fill_(float(step))
+                    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    ev0.record(stream)
+                    res = plan.integrate(n, seed=step, precision=prec, stream=stream.cuda_stream)
+                    ev1.record(stream)
+                    ev1.synchronize()
+                    if step >= 1:
+                        times.append(ev0.elapsed_time(ev1))
+            ms = sum(times) / len(times)
+            entry[tag] = {"value": n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                          "fp64_fallback_rate": res["fp64_fallback"] / n, "integral": res["integral"]}
+        entry["mixed_over_fp64"] = entry["mixed"]["value"] / entry["plain_fp64"]["value"]
+        out[name] = entry
+        plan.close()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -302,6 +337,7 @@ def main():
     ap.add_argument("--batched", default="scan", choices=["scan", "mixed", "none"],
                     help="the batched form's workload (one GPU runs it, rank 0 reports it)")
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--no-configs", action="store_true", help="skip the K4 and cube configurations")
     ap.add_argument("--batch-count", type=int, default=0,
                     help="only the first n integrals of the batch (profiler captures); 0: all")
     ap.add_argument("--batch-only", action="store_true",
@@ -457,6 +493,7 @@ def main():
     batched = None
     if args.batched != "none" and rank == 0:
         batched = batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local))
+    other = configs_section(args, ft, workloads, torch, flush) if (rank == 0 and not args.no_configs) else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -488,6 +525,7 @@ def main():
         "clocks": clocks,
         "cpu_baseline": cpu,
         "batched": batched,
+        "other_configs": other,
     }
     print(json.dumps(line), flush=True)
     if dist:
