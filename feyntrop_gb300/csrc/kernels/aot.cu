@@ -10,6 +10,8 @@
 //  ft_batch_item_states  stream states of the work items of a batch (one warp per
 //                      integral, GF(2) skip-ahead).
 //  ft_batch_finalize   per-integral sums of a batch's work items and FP64 pass.
+//  ft_warp_states      stream states of the warps of a sampling launch (one warp per
+//                      warp, GF(2) skip-ahead), so each thread skips only its lane.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -170,6 +172,20 @@ __global__ void __launch_bounds__(128) ft_batch_item_states(const item_prep* __r
     }
 }
 
+// one warp per output warp: the first lane's state of warp w of a sampling launch is
+// (T^S)^(32 w) base, i.e. the lane skip matrices of the bits of w shifted by 5
+__global__ void __launch_bounds__(128) ft_warp_states(const u64* __restrict__ lanepw, int lanebits, u64 s0, u64 s1,
+                                                      u64 s2, u64 s3, unsigned nwarps, u64* __restrict__ out)
+{
+    const unsigned w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = (int)(threadIdx.x & 31u);
+    if (w >= nwarps) return;   // the whole warp
+    u64 g[4] = {s0, s1, s2, s3};
+    for (int j = 0; j + 5 < lanebits; j++)
+        if ((w >> j) & 1u) warp_gf2_apply(lanepw + (size_t)(j + 5) * 1024, g, lane);
+    if (lane < 4) out[(size_t)w * 4 + lane] = word_of(g, lane);
+}
+
 // Per instance: the sums of its work items (double-double for the moment pairs) plus
 // the FP64 pass's sums (qacc, NULL for FP64 batches).  One thread per (instance,
 // moment pair or counter).  Slots: 8K moments as 4K (hi, lo) pairs, then kept,
@@ -295,6 +311,7 @@ cudaError_t noalloc_scratch(noalloc_layout* out)
     out->parts = (double*)(w + 2);
     out->queue = w + 2 + NOALLOC_PART_DOUBLES;
     out->lanepw = w + 2 + NOALLOC_PART_DOUBLES + 5 * (size_t)NOALLOC_QUEUE_ENTRIES;
+    out->warpst = out->lanepw + NOALLOC_LANE_WORDS;
     return cudaSuccess;
 }
 
@@ -319,6 +336,14 @@ cudaError_t launch_batch_finalize(const void* inst, int n, const double* parts, 
     const long long threads = (long long)n * (4 * K + 8);
     ft_batch_finalize<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>((const batch_inst_view*)inst, n, parts, K,
                                                                          qacc, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_warp_states(const u64* lanepw, int lanebits, const u64* base, unsigned nwarps, u64* out,
+                               cudaStream_t st)
+{
+    if (nwarps == 0) return cudaSuccess;
+    ft_warp_states<<<(nwarps + 3) / 4, 128, 0, st>>>(lanepw, lanebits, base[0], base[1], base[2], base[3], nwarps, out);
     return cudaGetLastError();
 }
 

@@ -22,21 +22,30 @@ cudaError_t launch_finalize(const double* parts, int nparts, int slots, int ndd,
 
 // Limits of the no-allocation path (ft_integrate_noalloc): per-block partial moments
 // for up to 2048 blocks of up to 136 slots (16 eps orders), 65536 FP64 hand-off
-// entries, lane skip matrices for up to 2^24 lanes.  About 5 MB per device.
+// entries, lane skip matrices for up to 2^24 lanes, the stream states of up to 32
+// warps per block.  About 7 MB per device.
 #define NOALLOC_MAX_BLOCKS 2048
 #define NOALLOC_MAX_SLOTS 136
 #define NOALLOC_PART_DOUBLES (NOALLOC_MAX_BLOCKS * NOALLOC_MAX_SLOTS)
 #define NOALLOC_QUEUE_ENTRIES 65536
 #define NOALLOC_MAX_LANE_BITS 24
 #define NOALLOC_LANE_WORDS (NOALLOC_MAX_LANE_BITS * 1024)
-#define NOALLOC_TOTAL_WORDS (2 + NOALLOC_PART_DOUBLES + 5 * NOALLOC_QUEUE_ENTRIES + NOALLOC_LANE_WORDS)
+#define NOALLOC_WARP_WORDS (NOALLOC_MAX_BLOCKS * 32 * 4)
+#define NOALLOC_TOTAL_WORDS \
+    (2 + NOALLOC_PART_DOUBLES + 5 * NOALLOC_QUEUE_ENTRIES + NOALLOC_LANE_WORDS + NOALLOC_WARP_WORDS)
 
 struct noalloc_layout {
     unsigned int* qcount;
     double* parts;
     unsigned long long* queue;
     unsigned long long* lanepw;
+    unsigned long long* warpst;
 };
+
+// stream states of the first lane of every warp of a launch: warp w starts at
+// (T^S)^(32 w) base, from the lane skip matrices lanepw[b] = (T^S)^(2^b), b < lanebits
+cudaError_t launch_warp_states(const unsigned long long* lanepw, int lanebits, const unsigned long long* base,
+                               unsigned nwarps, unsigned long long* out, cudaStream_t st);
 
 // device addresses inside the static scratch of the current device (first call per
 // device looks the symbol up)

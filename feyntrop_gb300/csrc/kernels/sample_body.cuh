@@ -1528,6 +1528,18 @@ static __device__ __noinline__ void block_reduce(double* vals /* ACC_SLOTS per t
     }
 }
 
+// stream state from 4 words (16-byte aligned)
+static __device__ __forceinline__ xo load_state(const u64* __restrict__ s)
+{
+    const ulonglong2 a = *(const ulonglong2*)s, b = *(const ulonglong2*)(s + 2);
+    xo g;
+    g.a = a.x;
+    g.b = a.y;
+    g.c = b.x;
+    g.d = b.y;
+    return g;
+}
+
 // ------------------------------------------------------------------ lane start states
 // state <- P_b state for every set bit b of `lane`, with P_b = (T^S)^(2^b) supplied by
 // the host (S = draws per lane).  The loop is uniform across the warp so that the
@@ -1885,11 +1897,12 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
 #if !FT_BATCH
 // ------------------------------------------------------------------ single-integral kernels
 // Thread t of the launch owns samples [t*chunk, min(nsamples, (t+1)*chunk)) counted
-// from the launch's first sample, whose stream state is (s0..s3).  Block b writes
-// its partial sums to acc_out[b * ACC_SLOTS ...].
+// from the launch's first sample.  warp_states[4w ..] is the stream state of the first
+// sample of warp w's lane 0 (computed by a preparation kernel), so a thread skips only
+// over its lane's offset.  Block b writes its partial sums to acc_out[b * ACC_SLOTS ...].
 extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
     const double* __restrict__ prm, const unsigned char* __restrict__ tab, const u64* __restrict__ lanepw,
-    int lanebits, u64 s0, u64 s1, u64 s2, u64 s3, u64 nsamples, u64 chunk, double* __restrict__ acc_out,
+    int lanebits, const u64* __restrict__ warp_states, u64 nsamples, u64 chunk, double* __restrict__ acc_out,
     u64* __restrict__ queue, unsigned int* __restrict__ qcount, unsigned int qcap,
     unsigned char* __restrict__ rec_order, double* __restrict__ rec_X, double* __restrict__ rec_R,
     unsigned char* __restrict__ rec_flags)
@@ -1898,12 +1911,8 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
     const table_ref tr = stage_table(smem, tab);
 
     const u32 t = blockIdx.x * blockDim.x + threadIdx.x;
-    xo g;
-    g.a = s0;
-    g.b = s1;
-    g.c = s2;
-    g.d = s3;
-    skip_lanes(g, t, lanepw, lanebits);
+    xo g = load_state(warp_states + (size_t)(t >> 5) * 4);
+    skip_lanes(g, t & 31u, lanepw, lanebits < 5 ? lanebits : 5);
 
     u64 first = (u64)t * chunk;
     u64 last = first + chunk;
@@ -1980,17 +1989,6 @@ static __device__ __forceinline__ int find_instance(const batch_inst* __restrict
             hi = mid - 1;
     }
     return lo;
-}
-
-static __device__ __forceinline__ xo load_state(const u64* __restrict__ s)
-{
-    const ulonglong2 a = *(const ulonglong2*)s, b = *(const ulonglong2*)(s + 2);
-    xo g;
-    g.a = a.x;
-    g.b = a.y;
-    g.c = b.x;
-    g.d = b.y;
-    return g;
 }
 
 extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample_batch(

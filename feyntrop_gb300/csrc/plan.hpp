@@ -67,6 +67,8 @@ struct ft_plan {
     unsigned int* d_qcount = nullptr;
     size_t qcap = 0;
     unsigned long long* d_lanepw = nullptr;
+    unsigned long long* d_warpst = nullptr;   // stream states of the warps of the last launch
+    size_t warpst_cap = 0;
     unsigned long long lanepw_S = 0;
     int lanepw_bits = 0;
     cudaStream_t stream = nullptr;
@@ -112,6 +114,7 @@ struct ft_plan {
         if (d_queue) cudaFree(d_queue);
         if (d_qcount) cudaFree(d_qcount);
         if (d_lanepw) cudaFree(d_lanepw);
+        if (d_warpst) cudaFree(d_warpst);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         if (stream) cudaStreamDestroy(stream);

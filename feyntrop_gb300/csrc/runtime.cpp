@@ -248,6 +248,16 @@ void ensure_queue(ft_plan& pl, size_t entries)
     pl.qcap = entries;
 }
 
+void ensure_warpst(ft_plan& pl, size_t nwarps)
+{
+    if (nwarps <= pl.warpst_cap) return;
+    if (pl.d_warpst) cudaFree(pl.d_warpst);
+    pl.d_warpst = nullptr;
+    pl.warpst_cap = 0;
+    cu(cudaMalloc(&pl.d_warpst, nwarps * 32), "cudaMalloc(warp stream states)");
+    pl.warpst_cap = nwarps;
+}
+
 void ensure_lanepw(ft_plan& pl, unsigned long long S, int bits, cudaStream_t st)
 {
     if (pl.d_lanepw && pl.lanepw_S == S && pl.lanepw_bits >= bits) return;
@@ -331,7 +341,13 @@ run_out run(ft_plan& pl, const ft_run_options& o, cudaStream_t st, const records
     cu(cudaMemsetAsync(pl.d_qcount, 0, 16, st), "cudaMemsetAsync");
     const ft::xstate base = ft::advance(ft::seed_state(o.seed), o.first_sample * draws);
 
-    unsigned long long s0 = base.s[0], s1 = base.s[1], s2 = base.s[2], s3 = base.s[3];
+    const unsigned nwarps = (unsigned)(((unsigned long long)g.blocks * ks.block + 31) / 32);
+    ensure_warpst(pl, nwarps);
+    cu(cudaEventRecord(pl.ev0, st), "cudaEventRecord");
+    cu(ft::launch_warp_states(pl.d_lanepw, g.lanebits, (const unsigned long long*)base.s, nwarps, pl.d_warpst, st),
+       "warp stream states");
+    out.launches++;
+    const unsigned long long* warpst = pl.d_warpst;
     unsigned long long nsamples = N, chunk = g.chunk;
     int lanebits = g.lanebits;
     unsigned int qcap = (unsigned int)pl.qcap;
@@ -351,9 +367,8 @@ run_out run(ft_plan& pl, const ft_run_options& o, cudaStream_t st, const records
         r_R = rec->R;
         r_flags = rec->flags;
     }
-    void* args[] = {&prm, &tab, &lanepw, &lanebits, &s0, &s1, &s2, &s3, &nsamples, &chunk, &parts, &queue, &qcount,
+    void* args[] = {&prm, &tab, &lanepw, &lanebits, &warpst, &nsamples, &chunk, &parts, &queue, &qcount,
                     &qcap, &r_order, &r_X, &r_R, &r_flags};
-    cu(cudaEventRecord(pl.ev0, st), "cudaEventRecord");
     ft::check(ft::drv().LaunchKernel(ks.sample, g.blocks, 1, 1, ks.block, 1, 1, ks.smem, (CUstream)st, args, nullptr),
               "launch ft_sample");
     out.launches++;
@@ -715,7 +730,10 @@ int ft_integrate_noalloc(ft_plan* pl, const ft_run_options* o, double* d_slots)
         cu(ft::launch_lane_powers(dev_state().tpow, g.chunk * draws, g.lanebits, sc.lanepw, st), "lane skip matrices");
         cu(cudaMemsetAsync(sc.qcount, 0, 8, st), "cudaMemsetAsync");
         const ft::xstate base = ft::advance(ft::seed_state(o->seed), o->first_sample * draws);
-        unsigned long long s0 = base.s[0], s1 = base.s[1], s2 = base.s[2], s3 = base.s[3];
+        const unsigned nwarps = (unsigned)(((unsigned long long)g.blocks * ks->block + 31) / 32);
+        cu(ft::launch_warp_states(sc.lanepw, g.lanebits, (const unsigned long long*)base.s, nwarps, sc.warpst, st),
+           "warp stream states");
+        const unsigned long long* warpst = sc.warpst;
         unsigned long long nsamples = N, chunk = g.chunk;
         int lanebits = g.lanebits;
         unsigned int qcap = NOALLOC_QUEUE_ENTRIES;
@@ -729,7 +747,7 @@ int ft_integrate_noalloc(ft_plan* pl, const ft_run_options* o, double* d_slots)
         double* r_X = nullptr;
         double* r_R = nullptr;
         uint8_t* r_flags = nullptr;
-        void* args[] = {&prm, &tab, &lanepw, &lanebits, &s0, &s1, &s2, &s3, &nsamples, &chunk, &parts, &queue, &qcount,
+        void* args[] = {&prm, &tab, &lanepw, &lanebits, &warpst, &nsamples, &chunk, &parts, &queue, &qcount,
                         &qcap, &r_order, &r_X, &r_R, &r_flags};
         ft::check(ft::drv().LaunchKernel(ks->sample, g.blocks, 1, 1, ks->block, 1, 1, ks->smem, (CUstream)st, args,
                                          nullptr),

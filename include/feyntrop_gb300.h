@@ -158,7 +158,7 @@ int ft_batch_get_info(const ft_batch* batch, ft_batch_info* info);
  * caller-owned DEVICE buffer of 8K+8 doubles: for eps order j and part p (0 Re, 1 Im)
  * [8j+4p .. +3] = sum f (hi, lo), sum f^2 (hi, lo); then kept, dropped, FP64
  * re-evaluated, exact sector steps, complete-pivoting factorisations.
- * Scratch is one static device array per GPU (about 5 MB, held until exit): at most
+ * Scratch is one static device array per GPU (about 7 MB, held until exit): at most
  * 2048 blocks, 16 eps orders and 65536 samples handed to the FP64 pass per call (more
  * are not evaluated: kept + dropped < N reports it).  The plan's kernels must already be
  * loaded by one ft_integrate call with the same precision.  The first call on a device
