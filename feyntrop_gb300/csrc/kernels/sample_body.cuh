@@ -1140,19 +1140,19 @@ static __device__ __forceinline__ f2 f2_neg(f2 a) { return f2_make(-a.hi, -a.lo)
 #endif
 // smallest pivot-to-row ratio accepted in the FP32 complex eliminations
 #ifndef PIVOT_GROWTH
-#define PIVOT_GROWTH 0.03f
+#define PIVOT_GROWTH 0.02f
 #endif
 // largest accepted (D/2) det L(|y|) / |det L(y)|: the complex determinant is a sum over
 // spanning trees with phases, and FP32 errors in it (and in psi^(-D/2)) grow by the
 // ratio of the phase-free sum to the result
 #ifndef DET_CANCEL
-#define DET_CANCEL 160.0f
+#define DET_CANCEL 400.0f
 #endif
 // largest accepted W (sum |terms of V|) / (|V| pivot growth) in the deformed integrand:
 // V^(-W) carries the FP32 error of the complex solves (grown by 1 / pivot growth),
 // amplified by the cancellation in V
 #ifndef V_AMPLIFY
-#define V_AMPLIFY 160.0f
+#define V_AMPLIFY 400.0f
 #endif
 #define RLN2_HI 1.44269502162933349609375f
 #define RLN2_LO 1.925963033500011e-8f
