@@ -1266,7 +1266,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
         pxi += v;
         mag += fabsf(v);
     }
-    if (!(pxi > V_CANCEL * mag)) {   // cancellation, or a sign the FP64 pass must judge
+    if (!(pxi > V_CANCEL * mag)) {   // cancellation, or a sign the FP64 pass must decide
         need64 = true;
         return false;
     }
