@@ -1,0 +1,96 @@
+"""Edge cases of the GPU path: the largest graphs of the suite's size range, many eps
+orders (the launch shape shrinks until the per-thread sums fit shared memory), empty
+and one-sample integrations, and a batch with an empty integral."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import feyntrop_gb300 as ft
+import oracle_lib as ol
+
+pytestmark = pytest.mark.gpu
+
+PINS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_pins.json")))
+
+
+def grid(a, b):
+    """a x b square grid (a b vertices, 2ab - a - b edges), Euclidean 2-point kinematics
+    between opposite corners, all masses 1, D = 4, 2 eps orders."""
+    idx = lambda i, j: i * b + j
+    g = []
+    for i in range(a):
+        for j in range(b):
+            if j + 1 < b:
+                g.append([[idx(i, j), idx(i, j + 1)], 1])
+            if i + 1 < a:
+                g.append([[idx(i, j), idx(i + 1, j)], 1])
+    V = a * b
+    P = [[0.0] * V for _ in range(V)]
+    P[0][0] = P[V - 1][V - 1] = -1.0
+    P[0][V - 1] = P[V - 1][0] = 1.0
+    return {"graph": g, "dimension": 4, "scalarproducts": P, "masses_sqr": [1.0] * len(g), "num_eps_terms": 2,
+            "lambda": 0, "N": 1000, "seed": 0}
+
+
+def test_seventeen_edge_graph_matches_the_oracle():
+    """3 x 4 grid: 17 edges, 12 vertices, 6 loops (table of 2^17 entries in global memory)."""
+    inp = grid(3, 4)
+    p = ft.Plan(inp)
+    ref = ol.Prepared(inp).samples(0, 0, 256)
+    for prec, tol in ((ft.FP64, 1e-9), (ft.MIXED, 2e-5)):
+        rec = p.records(256, seed=0, precision=prec)
+        assert (rec["order"] == ref["order"]).all()
+        ok = ~ref["dropped"]
+        scale = np.abs(ref["R"][ok]).max(axis=1)
+        err = np.abs(rec["R"][ok] - ref["R"][ok]).max(axis=1) / scale
+        queued = (rec["flags"][ok] & 2) != 0
+        assert err[~queued].max() < tol and err[queued].max(initial=0) < 1e-9, (prec, err.max())
+    a = p.integrate(200_000, seed=1, precision=ft.FP64)
+    b = p.integrate(200_000, seed=1, precision=ft.MIXED)
+    for j in range(2):
+        assert abs(a["integral"][j][0][0] - b["integral"][j][0][0]) <= 1e-3 * a["integral"][j][0][1]
+    p.close()
+
+
+def test_many_eps_orders_shrink_the_launch_and_agree():
+    """10 eps orders: 512 threads x 10 orders x 24 bytes of sums exceed shared memory,
+    so the block shrinks; mixed and FP64 still see the same samples."""
+    inp = dict(PINS["cases"]["C2_double_box"]["input"], num_eps_terms=10)
+    p = ft.Plan(inp)
+    a = p.integrate(300_000, seed=2, precision=ft.FP64)
+    b = p.integrate(300_000, seed=2, precision=ft.MIXED)
+    assert a["kept"] + a["dropped"] == 300_000 and b["kept"] + b["dropped"] == 300_000
+    for j in range(10):
+        for part in range(2):
+            x, dx = a["integral"][j][part]
+            y, dy = b["integral"][j][part]
+            assert abs(x - y) <= 0.05 * dx, (j, part, x, y, dx)
+    p.close()
+
+
+def test_empty_and_single_sample_integrations():
+    p = ft.Plan(PINS["cases"]["C1_K4"]["input"])
+    for prec in (ft.FP64, ft.MIXED):
+        r0 = p.integrate(0, precision=prec)
+        assert r0["kept"] == 0 and r0["dropped"] == 0
+        assert all(np.isnan(r0["integral"][j][0][0]) for j in range(p.K))   # 0/0, as the reference's stats
+        r1 = p.integrate(1, seed=3, precision=prec)
+        assert r1["kept"] + r1["dropped"] == 1
+        ref = ol.Prepared(PINS["cases"]["C1_K4"]["input"]).samples(3, 0, 1)
+        if not ref["dropped"][0]:
+            assert abs(r1["integral"][0][0][0] - ref["R"][0, 0].real) <= 1e-5 * abs(ref["R"][0, 0])
+    p.close()
+
+
+def test_batch_with_an_empty_integral():
+    ps = [ft.Plan(PINS["cases"][n]["input"]) for n in ("C1_K4", "C2_double_box")]
+    out = ft.Batch(ps, ft.MIXED).run([0, 100_000], seeds=[0, 4])
+    assert out[0]["kept"] == 0 and out[0]["dropped"] == 0
+    r = ps[1].integrate(100_000, seed=4, precision=ft.MIXED)
+    assert out[1]["kept"] == r["kept"]
+    x, dx = out[1]["integral"][0][0]
+    assert abs(x - r["integral"][0][0][0]) <= 1e-3 * dx
+    for p in ps:
+        p.close()
