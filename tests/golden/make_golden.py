@@ -183,6 +183,15 @@ def extra_cases():
              [[3, 4], 1]]
     c["wheel4_vacuum"] = {"graph": wheel, "dimension": 4, "scalarproducts": [[0.0] * 5 for _ in range(5)],
                           "masses_sqr": [1.0] * 8, "num_eps_terms": 2, "lambda": 0, "N": 1000, "seed": 0}
+
+    # non-unit, non-integer edge weights: the double box (Minkowski, deformed) and a
+    # Euclidean triangle
+    nus = [1, 1.5, 1, 2, 1, 0.5, 1]
+    c["nu_double_box"] = dict(c["C2_double_box"],
+                              graph=[[e[0], nu] for e, nu in zip(c["C2_double_box"]["graph"], nus)])
+    c["nu_triangle_eucl"] = {"graph": [[[0, 1], 0.7], [[1, 2], 1.3], [[2, 0], 2]], "dimension": 4,
+                             "scalarproducts": [[-1.0, 0.25, 0.75], [0.25, -2.0, 1.75], [0.75, 1.75, -2.5]],
+                             "masses_sqr": [0.5, 1.0, 1.5], "num_eps_terms": 3, "lambda": 0, "N": 1000, "seed": 0}
     return c
 
 
