@@ -394,6 +394,183 @@ static __device__ void robust_complex(const cx<double>* y, const double* prm, cx
     pphi = cmk(-tr.re, -tr.im);
 }
 
+// ------------------------------------------------------------------ robust derivatives
+// x-derivatives of phi/psi by the reference's route (srcs/feynman_integral.hpp:166-194,
+// 283-287; srcs/laplacian.hpp:14-99, 102-215), for samples where an edge's conductance
+// 1/x_e dwarfs the rest of the network between its ends: the fixed ground of the
+// unrolled path then leaves both ends floating together, and the potential and
+// resistance differences across the edge cancel.  Grounding the vertex with the
+// smallest sum of incident x (the reference's choice) ties such an edge to the ground.
+// Reduced Laplacian with that ground, LDL^T with diagonal pivoting, L^-1, L^-1 P L^-T,
+// then the derivatives as differences of their entries.  Runtime indices, out of line:
+// it runs for a few samples in 1e4 (edge weights below 1 make tiny x more frequent).
+static __device__ __noinline__ void robust_derivatives(const double* X, const double* Xi, const double* prm,
+                                                       double* dphi, double (*H)[FT_E])
+{
+    double XV[FT_V];
+#pragma unroll 1
+    for (int v = 0; v < FT_V; v++) XV[v] = 0.0;
+#pragma unroll 1
+    for (int e = 0; e < FT_E; e++) {
+        XV[FT_EK[e]] += X[e];
+        XV[FT_EL[e]] += X[e];
+    }
+    int gnd = 0;
+#pragma unroll 1
+    for (int v = 1; v < FT_V; v++)
+        if (XV[gnd] > XV[v]) gnd = v;
+    int map[FT_V];
+#pragma unroll 1
+    for (int v = 0; v < FT_V; v++) map[v] = v < gnd ? v : (v > gnd ? v - 1 : FT_N);
+    // reduced Laplacian A and contracted scalar products B (P from its rank split; the
+    // ground-V-1 row and column follow from momentum conservation)
+    double A[FT_N][FT_N], B[FT_N][FT_N];
+#pragma unroll 1
+    for (int i = 0; i < FT_N; i++)
+#pragma unroll 1
+        for (int j = 0; j < FT_N; j++) A[i][j] = 0.0;
+#pragma unroll 1
+    for (int e = 0; e < FT_E; e++) {
+        const int k = map[FT_EK[e]], l = map[FT_EL[e]];
+        if (k < FT_N) A[k][k] += Xi[e];
+        if (l < FT_N) A[l][l] += Xi[e];
+        if (k < FT_N && l < FT_N) {
+            A[k][l] -= Xi[e];
+            A[l][k] -= Xi[e];
+        }
+    }
+    auto Pfull = [&](int i, int j) -> double {
+        // P[i][j] of the V x V matrix with zero row and column sums
+        double s = 0.0;
+#pragma unroll 1
+        for (int r = 0; r < FT_RANK; r++) {
+            double qi = 0.0, qj = 0.0;
+            if (i < FT_N) {
+                qi = prm[P_Q + r * FT_N + i];
+            } else {
+#pragma unroll 1
+                for (int m = 0; m < FT_N; m++) qi -= prm[P_Q + r * FT_N + m];
+            }
+            if (j < FT_N) {
+                qj = prm[P_Q + r * FT_N + j];
+            } else {
+#pragma unroll 1
+                for (int m = 0; m < FT_N; m++) qj -= prm[P_Q + r * FT_N + m];
+            }
+            s += prm[P_SIG + r] * qi * qj;
+        }
+        return s;
+    };
+#pragma unroll 1
+    for (int v = 0; v < FT_V; v++) {
+        if (v == gnd) continue;
+#pragma unroll 1
+        for (int w = 0; w < FT_V; w++) {
+            if (w == gnd) continue;
+            B[map[v]][map[w]] = Pfull(v, w);
+        }
+    }
+    // A = P^T L D L^T P (diagonal pivoting); then A^-1 column by column into C
+    int perm[FT_N];
+#pragma unroll 1
+    for (int i = 0; i < FT_N; i++) perm[i] = i;
+#pragma unroll 1
+    for (int k = 0; k < FT_N; k++) {
+        int pk = k;
+#pragma unroll 1
+        for (int i = k + 1; i < FT_N; i++)
+            if (fabs(A[i][i]) > fabs(A[pk][pk])) pk = i;
+        if (pk != k) {
+#pragma unroll 1
+            for (int j = 0; j < FT_N; j++) {
+                const double t = A[k][j];
+                A[k][j] = A[pk][j];
+                A[pk][j] = t;
+            }
+#pragma unroll 1
+            for (int j = 0; j < FT_N; j++) {
+                const double t = A[j][k];
+                A[j][k] = A[j][pk];
+                A[j][pk] = t;
+            }
+            const int t = perm[k];
+            perm[k] = perm[pk];
+            perm[pk] = t;
+        }
+        const double dk = A[k][k];
+        // Schur update of the whole (symmetric) trailing block, so that later pivot
+        // swaps see current values in both triangles; row k keeps the unscaled column
+#pragma unroll 1
+        for (int i = k + 1; i < FT_N; i++) {
+            const double f = A[i][k] / dk;
+#pragma unroll 1
+            for (int j = k + 1; j < FT_N; j++) A[i][j] -= f * A[k][j];
+        }
+#pragma unroll 1
+        for (int i = k + 1; i < FT_N; i++) A[i][k] /= dk;
+    }
+    // columns of the inverse: solve L D L^T y = P e_c; C[perm[i]][c] = y_i
+    double C[FT_N][FT_N];
+#pragma unroll 1
+    for (int c = 0; c < FT_N; c++) {
+        double y[FT_N];
+#pragma unroll 1
+        for (int i = 0; i < FT_N; i++) {
+            double t = perm[i] == c ? 1.0 : 0.0;
+#pragma unroll 1
+            for (int j = 0; j < i; j++) t -= A[i][j] * y[j];
+            y[i] = t;
+        }
+#pragma unroll 1
+        for (int i = 0; i < FT_N; i++) y[i] /= A[i][i];
+#pragma unroll 1
+        for (int i = FT_N - 1; i >= 0; i--)
+#pragma unroll 1
+            for (int j = i + 1; j < FT_N; j++) y[i] -= A[j][i] * y[j];
+#pragma unroll 1
+        for (int i = 0; i < FT_N; i++) C[perm[i]][c] = y[i];
+    }
+    // S = C B C^T (into A, reusing it)
+#pragma unroll 1
+    for (int i = 0; i < FT_N; i++)
+#pragma unroll 1
+        for (int j = 0; j < FT_N; j++) {
+            double t = 0.0;
+#pragma unroll 1
+            for (int k = 0; k < FT_N; k++) t += C[i][k] * B[k][j];
+            A[i][j] = t;
+        }
+#pragma unroll 1
+    for (int i = 0; i < FT_N; i++)
+#pragma unroll 1
+        for (int j = 0; j < FT_N; j++) {
+            double t = 0.0;
+#pragma unroll 1
+            for (int k = 0; k < FT_N; k++) t += A[i][k] * C[j][k];
+            B[i][j] = t;
+        }
+    // derivatives (srcs/laplacian.hpp:127-213): differences of S = B and of C
+    auto S = [&](int i, int j) -> double { return (i == FT_N || j == FT_N) ? 0.0 : B[i][j]; };
+    auto T = [&](int i, int j) -> double { return (i == FT_N || j == FT_N) ? 0.0 : C[i][j]; };
+#pragma unroll 1
+    for (int a = 0; a < FT_E; a++) {
+        const int ka = map[FT_EK[a]], la = map[FT_EL[a]];
+        const double s = S(ka, ka) + S(la, la) - 2.0 * S(ka, la);
+        const double t = T(ka, ka) + T(la, la) - 2.0 * T(ka, la);
+        const double xa = Xi[a] * Xi[a];
+        const double xas = xa * s;
+        dphi[a] = -xas;
+        H[a][a] = 2.0 * xas * (Xi[a] - xa * t);
+#pragma unroll 1
+        for (int b = a + 1; b < FT_E; b++) {
+            const int kb = map[FT_EK[b]], lb = map[FT_EL[b]];
+            const double s2 = S(ka, kb) + S(la, lb) - S(ka, lb) - S(la, kb);
+            const double t2 = T(ka, kb) + T(la, lb) - T(ka, lb) - T(la, kb);
+            H[a][b] = -2.0 * xa * (Xi[b] * Xi[b]) * s2 * t2;
+        }
+    }
+}
+
 // ------------------------------------------------------------------ sector draw, FP64
 struct table_ref {
     const void* w;              // staged copies (shared memory): w, Jr, 1/r in the working precision
@@ -785,6 +962,7 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
     auto Gx = [&](int i, int j) -> double { return (i == FT_V - 1 || j == FT_V - 1) ? 0.0 : G[i][j]; };
     double dphi[FT_E];
     double H[FT_E][FT_E];
+    bool cancel = false;
 #pragma unroll
     for (int a = 0; a < FT_E; a++) {
         const int ka = FT_EK[a], la = FT_EL[a];
@@ -792,6 +970,8 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
 #pragma unroll
         for (int r = 0; r < FT_RANK; r++) s += prm[P_SIG + r] * hb[r][a] * hb[r][a];
         const double t = Gx(ka, ka) + Gx(la, la) - 2.0 * Gx(ka, la);
+        // an edge whose ends float together: its resistance difference cancels
+        cancel |= ka != FT_V - 1 && !(t > 1e-7 * (Gx(ka, ka) + Gx(la, la)));
         const double xa = Xi[a] * Xi[a];
         const double xas = xa * s;
         dphi[a] = -xas;
@@ -806,6 +986,10 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
             H[a][b] = -2.0 * xa * (Xi[b] * Xi[b]) * s2 * t2;
         }
     }
+    if (cancel) {
+        robust_derivatives(X, Xi, prm, dphi, H);
+        robust = true;
+    }
     // deformation x -> x exp(i theta), theta = -lambda (d(phi/psi)/dx + m^2)
     double theta[FT_E];
     cx<double> cX[FT_E], cy[FT_E];
@@ -814,6 +998,7 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
         theta[e] = (dphi[e] + prm[P_M2 + e]) * kappa;
+        FT_DBG(40 + e, theta[e]);
         double sn, cs;
         sincos(theta[e], &sn, &cs);
         cX[e] = cmk(X[e] * cs, X[e] * sn);
@@ -968,7 +1153,7 @@ static __device__ __forceinline__ df df_of(f2 x)
 // combinations t, and the Minkowski products s.  Outputs theta and the upper
 // triangle of H in FP32.  pd: the parameter block as two-float pairs.
 static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f2* XiT, const float* pd, df* theta_out,
-                                                      float (*H_out)[FT_E])
+                                                      float (*H_out)[FT_E], bool& cancel)
 {
     df c[FT_N][FT_N], g[FT_N];
 #pragma unroll
@@ -1065,6 +1250,8 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
             s = df_fma(sig_hb[r], hb[r][a2], s);
         }
         const df t = df_sub(df_add(Gx(ka, ka), Gx(la, la)), df_add(Gx(ka, la), Gx(ka, la)));
+        // an edge whose ends float together: the FP64 pass takes the sample
+        cancel |= ka != FT_V - 1 && !(df_f(t) > 1e-7f * (df_f(Gx(ka, ka)) + df_f(Gx(la, la))));
         const df xi = df_of(XiT[a2]);
         const df xa = df_mul(xi, xi);
         const df xas = df_mul(xa, s);
@@ -1297,7 +1484,12 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     // which cancel in FP32 for a sizeable fraction of sectors; this block runs in FP64.
     df theta[FT_E];
     float H[FT_E][FT_E];
-    derivatives_df(Xi, Xi2, pd, theta, H);
+    bool cancel = false;
+    derivatives_df(Xi, Xi2, pd, theta, H, cancel);
+    if (cancel) {
+        need64 = true;
+        return false;
+    }
     cx<float> cX[FT_E], cy[FT_E];
     // phase sums in two-float: sum theta and nu . theta
     f2 xnu = f2_make(0.0f, 0.0f), thsum = f2_make(0.0f, 0.0f);

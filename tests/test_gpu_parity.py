@@ -25,10 +25,10 @@ N_REC = 4096
 # per-sample relative error, |R_gpu - R_oracle| / max_j |R_oracle_j| of the sample
 FP64_MEDIAN_TOL = 1e-12
 # In ill-conditioned sectors the reference's own FP64 algorithm (pivoted LDLT of the
-# Laplacian, derivatives from its inverse) loses up to ~2e-7; the GPU's conductance-form
-# elimination stays within ~1e-10 of a 50-digit evaluation there
-# (test_fp64_disagreements_refereed_at_high_precision).
-FP64_MAX_TOL = 1e-6
+# Laplacian, derivatives from its inverse) loses up to ~2e-7 with unit edge weights and
+# ~6e-6 with weights below one; the GPU stays within ~1e-10 of a 50-digit evaluation
+# there (test_fp64_disagreements_refereed_at_high_precision).
+FP64_MAX_TOL = 1e-5
 MIXED_P999_TOL = 1e-5    # 99.9 % of the samples
 # single samples of the random box-pentagon kinematics (invariants uniform in
 # [-10, 10]) reach ~1.6e-5: moderately small complex pivots and large Jacobian
@@ -80,7 +80,7 @@ def test_mixed_samples_match_oracle(name):
     assert err.max() < MIXED_MAX_TOL
 
 
-@pytest.mark.parametrize("name", ["C2_double_box", "2L_4pt_ladder", "C3_box_pentagon_1"])
+@pytest.mark.parametrize("name", ["C2_double_box", "2L_4pt_ladder", "C3_box_pentagon_1", "nu_double_box"])
 def test_fp64_disagreements_refereed_at_high_precision(name):
     mp = pytest.importorskip("mpmath")
     import hp_truth
