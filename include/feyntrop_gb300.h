@@ -58,7 +58,7 @@ int ft_plan_create(const ft_problem* problem, ft_plan** out);
 void ft_plan_destroy(ft_plan* plan);
 
 /* ft_plan_create for many problems at once on all host threads (kinematic scans,
- * batches).  out[i] is NULL where problem i failed; status[i] (may be NULL) holds each
+ * batches; the reference prepares one input per process, srcs/feyntrop.cpp:143-158).  out[i] is NULL where problem i failed; status[i] (may be NULL) holds each
  * problem's code.  Returns FT_OK, or the code of the first failure (its message, with
  * the problem's index, in ft_last_error()). */
 int ft_plans_create(const ft_problem* problems, int32_t count, ft_plan** out, int32_t* status);
@@ -123,7 +123,8 @@ int ft_integrate(ft_plan* plan, const ft_run_options* opts, ft_result* result);
 int ft_integrate_batch(ft_plan* const* plans, int32_t count, const ft_run_options* opts, ft_result* results);
 
 /* A batch: many integrals (any mix of graphs, kinematics, seeds and sample counts) run
- * by one CUDA graph launch.  Integrals of one kernel class (same topology, eps orders,
+ * by one CUDA graph launch (each integral replaces one feynman_integral_estimate call,
+ * srcs/feynman_integral.hpp:30-41).  Integrals of one kernel class (same topology, eps orders,
  * regime) share one persistent sampling launch whose blocks take work items of
  * consecutive samples from a device counter; classes run side by side.  The batch
  * copies the plans' parameters and tables at creation; the plans must outlive it (their
@@ -170,7 +171,9 @@ int ft_integrate_noalloc(ft_plan* plan, const ft_run_options* opts, double* d_sl
  * real_only marks integrals whose imaginary part the reference reports as (0, 0). */
 int ft_finalize_moments(const ft_moments* moments, int32_t num_eps_terms, int32_t real_only, ft_result* result);
 
-/* Per-sample records of samples first_sample .. +N-1 (parity checks): removal order
+/* Per-sample records of samples first_sample .. +N-1 (parity checks; no counterpart in
+ * the reference, whose per-sample values exist only inside its loop,
+ * srcs/feynman_integral.hpp:162-362): removal order
  * (N x E bytes), X before rescaling (N x E), integrand per eps order (N x K x 2:
  * re, im) and flags (bit 0 dropped, 1 re-evaluated in FP64, 2 exact sector step,
  * 3 complete-pivoting LU).  Any pointer may be NULL. */
@@ -189,14 +192,14 @@ void ft_free(void* p);
 int ft_subgraph_table(const ft_problem* problem, double* Jr, double* r, uint8_t* mm, uint8_t* loops,
                       ft_plan_info* info);
 
-/* Host preprocessing plus run-time compilation of the sampling kernels for this
- * problem's topology (FP64 and, if requested, mixed; with FT_PRECOMPILE_BATCH or'ed
+/* No counterpart in the reference (it has no device code).  Host preprocessing plus
+ * run-time compilation of the sampling kernels for this problem's topology (FP64 and, if requested, mixed; with FT_PRECOMPILE_BATCH or'ed
  * into precision also the batch kernels), without touching a device: warms the kernel
  * cache.  *seconds receives the compile time (0 when cached). */
 #define FT_PRECOMPILE_BATCH 0x100
 int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds);
 
-/* Autotuner: times the sampling kernels of this plan's kernel class (topology, eps
+/* Autotuner (no counterpart in the reference): times the sampling kernels of this plan's kernel class (topology, eps
  * orders, regime, precision) under candidate launch shapes (threads per block, blocks
  * per SM given to the register allocator, code-size variants), `samples` samples per
  * trial, then the batch work-item size (samples per thread: 32 .. 256) under the chosen
@@ -213,7 +216,7 @@ typedef struct {
 } ft_tune_result;
 int ft_autotune(ft_plan* plan, int32_t precision, uint64_t samples, ft_tune_result* out);
 
-/* Measured FP32 and FP64 FMA issue rates of the current device in TFLOP/s (an
+/* No counterpart in the reference.  Measured FP32 and FP64 FMA issue rates of the current device in TFLOP/s (an
  * FMA-chain probe kernel; the denominators of the sampling kernels' roofline). */
 int ft_device_peaks(double* fp32_tflops, double* fp64_tflops);
 
