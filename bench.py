@@ -294,6 +294,30 @@ def configs_section(args, ft, workloads, torch, flush):
     return out
 
 
+def lambda_section(ft, workloads, N):
+    """The deformation parameter of the double box chosen by pilot runs
+    (ft.choose_lambda), and the time to a 1e-4 relative error of Re I0 at the chosen
+    lambda against the benchmark's lambda = 0.5 (same rate measurement: one timed
+    mixed integration of N samples at each)."""
+    inp = workloads.double_box(N=1000)
+    (lam, rel, table), = ft.choose_lambda([inp], candidates=(0.05, 0.1, 0.2, 0.3, 0.5, 0.8), pilot=10 ** 6)
+    out = {"candidates_relative_error": {str(k): v for k, v in table.items()}, "chosen": lam}
+    for tag, l in (("chosen", lam), ("benchmark", 0.5)):
+        p = ft.Plan(dict(inp, **{"lambda": l}))
+        p.integrate(N // 10, seed=0, precision=ft.MIXED)
+        r = p.integrate(N, seed=1, precision=ft.MIXED)
+        rate = N / (r["kernel_ms"] * 1e-3)
+        (re, dre), (im, dim) = r["integral"][0]
+        spread = dre * math.sqrt(N)
+        target = 1e-4 * abs(re)
+        out[tag] = {"lambda": l, "integral_eps0": [[re, dre], [im, dim]], "samples_per_second": rate,
+                    "time_to_1e-4_relative_s": (spread / target) ** 2 / rate if target > 0 else None}
+        p.close()
+    c, b_ = out["chosen"]["time_to_1e-4_relative_s"], out["benchmark"]["time_to_1e-4_relative_s"]
+    out["speedup_time_to_target"] = b_ / c if (b_ and c) else None
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -494,6 +518,7 @@ def main():
     if args.batched != "none" and rank == 0:
         batched = batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local))
     other = configs_section(args, ft, workloads, torch, flush) if (rank == 0 and not args.no_configs) else None
+    lam = lambda_section(ft, workloads, 10 ** 8) if (rank == 0 and not args.no_configs) else None
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": True, "scaling": "weak",
@@ -526,6 +551,7 @@ def main():
         "cpu_baseline": cpu,
         "batched": batched,
         "other_configs": other,
+        "lambda_choice": lam,
     }
     print(json.dumps(line), flush=True)
     if dist:

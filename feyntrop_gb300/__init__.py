@@ -384,6 +384,44 @@ class Batch:
             pass
 
 
+def choose_lambda(inputs, candidates=(0.05, 0.1, 0.2, 0.3, 0.5, 0.8), pilot=200_000, precision=MIXED, seed=0,
+                  eps_order=0):
+    """Deformation parameter per integral from pilot runs: for every candidate lambda,
+    all inputs (the low-level JSON dicts) at that lambda integrated as one batch with
+    `pilot` samples; per input the lambda with the smallest relative standard error of
+    its eps order `eps_order` (max over Re and Im, relative to the larger of |Re|, |Im|).
+    The contour deformation does not change the integral, only the spread of the
+    integrand (srcs/feynman_integral.hpp:288-291), so the best lambda shortens the time
+    to a target error by the square of the error ratio.  Inputs whose plan the checks
+    reject at some lambda skip it.  Returns [(lambda, relative error, {lambda: relative
+    error})] per input."""
+    table = [dict() for _ in inputs]
+    for lam in candidates:
+        plans = create_plans([dict(x, **{"lambda": lam}) for x in inputs], skip_failed=True)
+        idx = [i for i, p in enumerate(plans) if p is not None]
+        if not idx:
+            continue
+        b = Batch([plans[i] for i in idx], precision)
+        out = b.run(pilot, seeds=seed)
+        b.close()
+        for k, i in enumerate(idx):
+            (re, dre), (im, dim) = out[k]["integral"][eps_order]
+            scale = max(abs(re), abs(im))
+            rel = max(dre, dim) / scale if scale > 0 else math.inf
+            table[i][lam] = rel if math.isfinite(rel) else math.inf
+        for p in plans:
+            if p is not None:
+                p.close()
+    best = []
+    for t in table:
+        if not t:
+            best.append((None, math.inf, t))
+            continue
+        lam = min(t, key=lambda l: (t[l], l))
+        best.append((lam, t[lam], t))
+    return best
+
+
 def integrate_batch(plans, N, seeds=0, precision=MIXED, first_samples=0):
     """ft_integrate_batch: a transient batch over the plans (same precision for all)."""
     n = len(plans)

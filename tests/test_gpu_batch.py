@@ -183,3 +183,21 @@ def test_run_to_accuracy_reaches_the_target_on_the_same_samples(plans):
         single = plans[i].integrate(r["samples"], seed=3, precision=ft.MIXED)
         assert_same(r, single, ft.MIXED, NAMES[i])
     b.close()
+
+
+def test_choose_lambda_finds_the_low_variance_contour():
+    """The double box at lambda = 0.5 (the benchmark's value) has a per-sample spread
+    that swamps the integral; pilot runs pick a lambda whose estimate is precise, and
+    the integral at it agrees with the estimates at neighbouring lambdas."""
+    inp = workloads.double_box(N=1000)
+    (lam, rel, table), = ft.choose_lambda([inp], candidates=(0.1, 0.2, 0.3, 0.5), pilot=300_000)
+    assert lam in (0.1, 0.2, 0.3) and rel < 0.05 < table[0.5], table
+    vals = []
+    for l in (0.1, 0.2, 0.3):
+        p = ft.Plan(dict(inp, **{"lambda": l}))
+        r = p.integrate(2_000_000, seed=1, precision=ft.MIXED)
+        vals.append(r["integral"][0])
+        p.close()
+    (re0, d0), (im0, e0) = vals[1]
+    for (re, d), (im, e) in vals:
+        assert abs(re - re0) <= 5 * (d + d0) and abs(im - im0) <= 5 * (e + e0), vals
