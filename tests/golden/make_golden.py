@@ -192,6 +192,23 @@ def extra_cases():
     c["nu_triangle_eucl"] = {"graph": [[[0, 1], 0.7], [[1, 2], 1.3], [[2, 0], 2]], "dimension": 4,
                              "scalarproducts": [[-1.0, 0.25, 0.75], [0.25, -2.0, 1.75], [0.75, 1.75, -2.5]],
                              "masses_sqr": [0.5, 1.0, 1.5], "num_eps_terms": 3, "lambda": 0, "N": 1000, "seed": 0}
+
+    # odd dimension (half-integer degree of divergence), and a massless box in D = 6
+    # with off-shell external legs (Minkowski, deformed)
+    c["D3_triangle_eucl"] = dict(c["nu_triangle_eucl"], dimension=3,
+                                 graph=[[[0, 1], 1], [[1, 2], 1], [[2, 0], 1]])
+    box_sp = {(0, 0): 1.0, (1, 1): 2.0, (2, 2): 1.5, (0, 1): 3.0, (1, 2): -2.0, (0, 2): 0.5}
+    n = 3
+    P = [[0.0] * 4 for _ in range(4)]
+    for (i, j), v in box_sp.items():
+        P[i][j] = P[j][i] = v
+    for j in range(n):
+        P[n][j] = -sum(P[i][j] for i in range(n))
+    for i in range(n + 1):
+        P[i][n] = -sum(P[i][j] for j in range(n))
+    c["massless_box_D6"] = {"graph": [[[0, 1], 1], [[1, 2], 1], [[2, 3], 1], [[3, 0], 1]], "dimension": 6,
+                            "scalarproducts": P, "masses_sqr": [0.0] * 4, "num_eps_terms": 2, "lambda": 0.5,
+                            "N": 1000, "seed": 0}
     return c
 
 
