@@ -87,22 +87,46 @@ __device__ __forceinline__ void dd_add(double& ah, double& al, double bh, double
     al = err - (ah - s);
 }
 
-// one thread per slot pair (moments) or slot (counters)
-__global__ void ft_finalize_parts(const double* __restrict__ parts, int nparts, int slots, int ndd,
-                                  double* __restrict__ out)
+// one block per slot pair (moments) or slot (counters): the block's threads take the
+// parts in turn, then a double-double (or plain) tree across the block
+__global__ void __launch_bounds__(256) ft_finalize_parts(const double* __restrict__ parts, int nparts, int slots,
+                                                         int ndd, double* __restrict__ out)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double sh[8], sl[8];
+    const int u = blockIdx.x;
     const int npairs = ndd / 2;
-    if (t < npairs) {
-        double h = 0.0, l = 0.0;
-        for (int p = 0; p < nparts; p++) dd_add(h, l, parts[(size_t)p * slots + 2 * t], parts[(size_t)p * slots + 2 * t + 1]);
-        out[2 * t] = h;
-        out[2 * t + 1] = l;
-    } else if (t < npairs + (slots - ndd)) {
-        const int s = ndd + (t - npairs);
-        double v = 0.0;
-        for (int p = 0; p < nparts; p++) v += parts[(size_t)p * slots + s];
-        out[s] = v;
+    const bool pair = u < npairs;
+    const int s = pair ? 2 * u : ndd + (u - npairs);
+    double h = 0.0, l = 0.0;
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
+        if (pair)
+            dd_add(h, l, parts[(size_t)p * slots + s], parts[(size_t)p * slots + s + 1]);
+        else
+            h += parts[(size_t)p * slots + s];
+    }
+    for (int off = 16; off; off >>= 1) {
+        const double oh = __shfl_down_sync(0xffffffffu, h, off), ol = __shfl_down_sync(0xffffffffu, l, off);
+        if (pair)
+            dd_add(h, l, oh, ol);
+        else
+            h += oh;
+    }
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        sh[w] = h;
+        sl[w] = l;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double H = sh[0], L = sl[0];
+        for (int i = 1; i < (int)(blockDim.x >> 5); i++) {
+            if (pair)
+                dd_add(H, L, sh[i], sl[i]);
+            else
+                H += sh[i];
+        }
+        out[s] = H;
+        if (pair) out[s + 1] = L;
     }
 }
 
@@ -349,8 +373,8 @@ cudaError_t launch_warp_states(const u64* lanepw, int lanebits, const u64* base,
 
 cudaError_t launch_finalize(const double* parts, int nparts, int slots, int ndd, double* out, cudaStream_t st)
 {
-    const int threads = ndd / 2 + (slots - ndd);
-    ft_finalize_parts<<<(threads + 127) / 128, 128, 0, st>>>(parts, nparts, slots, ndd, out);
+    const int units = ndd / 2 + (slots - ndd);
+    ft_finalize_parts<<<units, 256, 0, st>>>(parts, nparts, slots, ndd, out);
     return cudaGetLastError();
 }
 

@@ -2125,9 +2125,14 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue(
     unsigned char* __restrict__ rec_flags)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    const table_ref tr = stage_table(smem, tab);
     unsigned int n = *qcount;
     if (n > qcap) n = qcap;
+    if ((size_t)blockIdx.x * blockDim.x >= n) {
+        // no entry for this block (the whole block leaves together): zero sums
+        for (int s = threadIdx.x; s < ACC_SLOTS; s += blockDim.x) acc_out[(size_t)blockIdx.x * ACC_SLOTS + s] = 0.0;
+        return;
+    }
+    const table_ref tr = stage_table(smem, tab);
     accum A;
     A.init(smem + ACC_SMEM_OFFSET);
     for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {

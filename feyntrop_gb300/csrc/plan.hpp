@@ -66,11 +66,19 @@ struct ft_plan {
     unsigned long long* d_queue = nullptr;
     unsigned int* d_qcount = nullptr;
     size_t qcap = 0;
-    unsigned long long* d_lanepw = nullptr;
+    // lane skip matrices for the last few per-thread strides S (alternating precisions
+    // or sample counts reuse them): 64 matrices of 8 KB each per entry
+    struct lane_entry {
+        unsigned long long* d = nullptr;
+        unsigned long long S = 0;
+        int bits = 0;
+        unsigned long long used = 0;
+    };
+    lane_entry lanes[4];
+    unsigned long long lane_clock = 0;
+    unsigned long long* d_lanepw = nullptr;   // the entry of the current launch
     unsigned long long* d_warpst = nullptr;   // stream states of the warps of the last launch
     size_t warpst_cap = 0;
-    unsigned long long lanepw_S = 0;
-    int lanepw_bits = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;
@@ -113,7 +121,8 @@ struct ft_plan {
         if (h_final) cudaFreeHost(h_final);
         if (d_queue) cudaFree(d_queue);
         if (d_qcount) cudaFree(d_qcount);
-        if (d_lanepw) cudaFree(d_lanepw);
+        for (lane_entry& e : lanes)
+            if (e.d) cudaFree(e.d);
         if (d_warpst) cudaFree(d_warpst);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);

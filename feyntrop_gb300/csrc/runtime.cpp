@@ -258,13 +258,27 @@ void ensure_warpst(ft_plan& pl, size_t nwarps)
     pl.warpst_cap = nwarps;
 }
 
-void ensure_lanepw(ft_plan& pl, unsigned long long S, int bits, cudaStream_t st)
+// points pl.d_lanepw at the lane skip matrices (T^S)^(2^b), b < bits; returns true when
+// it had to compute them (one launch), false when a cached entry served
+bool ensure_lanepw(ft_plan& pl, unsigned long long S, int bits, cudaStream_t st)
 {
-    if (pl.d_lanepw && pl.lanepw_S == S && pl.lanepw_bits >= bits) return;
-    if (!pl.d_lanepw) cu(cudaMalloc(&pl.d_lanepw, (size_t)64 * 1024 * 8), "cudaMalloc(lane skip matrices)");
-    cu(ft::launch_lane_powers(dev_state().tpow, S, bits, pl.d_lanepw, st), "lane skip matrices");
-    pl.lanepw_S = S;
-    pl.lanepw_bits = bits;
+    pl.lane_clock++;
+    ft_plan::lane_entry* victim = &pl.lanes[0];
+    for (ft_plan::lane_entry& e : pl.lanes) {
+        if (e.d && e.S == S && e.bits >= bits) {
+            e.used = pl.lane_clock;
+            pl.d_lanepw = e.d;
+            return false;
+        }
+        if (e.used < victim->used) victim = &e;
+    }
+    if (!victim->d) cu(cudaMalloc(&victim->d, (size_t)64 * 1024 * 8), "cudaMalloc(lane skip matrices)");
+    cu(ft::launch_lane_powers(dev_state().tpow, S, bits, victim->d, st), "lane skip matrices");
+    victim->S = S;
+    victim->bits = bits;
+    victim->used = pl.lane_clock;
+    pl.d_lanepw = victim->d;
+    return true;
 }
 
 struct launch_geometry {
@@ -330,8 +344,7 @@ run_out run(ft_plan& pl, const ft_run_options& o, cudaStream_t st, const records
     out.acc.assign(pl.slots(), 0.0);
     if (N == 0) return out;
 
-    ensure_lanepw(pl, g.chunk * draws, g.lanebits, st);
-    out.launches++;
+    if (ensure_lanepw(pl, g.chunk * draws, g.lanebits, st)) out.launches++;
     const unsigned qblocks = prec ? (unsigned)(dev_state().sms * std::max(1, k64->queue_blocks_per_sm)) : 0;
     ensure_parts(pl, g.blocks + qblocks);
     if (prec) {
