@@ -47,16 +47,42 @@ METRIC = "samples/s on 1 GB300: mixed-prec batched vs plain FP64 at <=1e-5 rel e
 UNIT = "samples/s"
 
 
-def algorithmic_flops(E, V, K, deformed):
-    """Floating-point operations per sample of the reference's algorithm (transcendentals
-    counted once each): cut scan, sector, Laplacian LDLT and solve, Minkowski: inverse,
-    L^-1 P L^-T, derivatives, complex LU and solve, Jacobian LU, complex pow/log."""
+def _formula_flops(E, V, K, deformed):
+    """Estimated floating-point operations per sample of the reference's algorithm
+    (transcendentals once each), for a class the counted table does not hold."""
     n = V - 1
     f = E * (E + 1) + 8 * E + 2 * n ** 3 / 3 + 2 * n ** 3 + V * V + (E + 3) + 2
     if deformed:
         f += 2 * n ** 3 + 4 * n ** 3 + 5 * E * E + 8 * n ** 3 / 3 + 8 * n ** 3 + 8 * E ** 3 / 3 + E + 4
-    f += 4 * K
-    return f
+    return f + 4 * K
+
+
+def _flop_table():
+    """profiles/flop_counts.txt: operations per sample counted by running the oracle's
+    restatement of the reference's loop with an operation-counting scalar (lines:
+    workload E V K deformed add mul div sqrt trans flops cmp samples)."""
+    rows = {}
+    path = os.path.join(HERE, "profiles", "flop_counts.txt")
+    if os.path.exists(path):
+        for line in open(path):
+            f = line.split()
+            if line.startswith("#") or len(f) < 13:
+                continue
+            rows[(int(f[1]), int(f[2]), bool(int(f[4])))] = (int(f[3]), float(f[10]), f[0])
+    return rows
+
+
+FLOP_TABLE = _flop_table()
+
+
+def algorithmic_flops(E, V, K, deformed):
+    """(flops per sample, source): the counted figure of this topology class and regime
+    (each further eps order: 8 flops deformed, 2 undeformed), else the estimate."""
+    row = FLOP_TABLE.get((E, V, bool(deformed)))
+    if row is None:
+        return _formula_flops(E, V, K, deformed), "estimate"
+    k0, flops, name = row
+    return flops + (K - k0) * (8 if deformed else 2), "counted (%s)" % name
 
 
 def dram_traffic(key):
@@ -191,6 +217,9 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
     plans = ft.create_plans(inputs)
     t_plans = time.perf_counter() - t0
     Ns = [x["N"] for x in inputs]
+    fp32_peak, fp64_peak = ft.device_peaks()
+    fl = [algorithmic_flops(p.E, p.V, p.K, bool(p.info["deformed"])) for p in plans]
+    flops, flop_src = [f for f, _ in fl], [s_ for _, s_ in fl]
     stream = torch.cuda.Stream()
     out = {"workload": name, "integrals": len(plans), "redrawn": redrawn, "samples_per_run": sum(Ns),
            "seconds_preprocessing_all": t_plans}
@@ -215,11 +244,17 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
         info = b.info()
         ms = sum(times) / len(times)
         rates[tag] = sum(n) / (ms * 1e-3)
+        tf = sum(f * k for f, k in zip(flops, n)) / (ms * 1e-3) / 1e12
+        peak = fp32_peak if prec == ft.MIXED else fp64_peak
         out[tag] = {"value": rates[tag], "unit": UNIT, "ms_per_run": ms, "runs": len(times),
                     "sample_scale": scale, "samples_per_run": sum(n), "classes": info["num_classes"],
                     "kernel_launches_per_run": info["kernel_launches"], "graph_launches_per_run": 1,
                     "graph_captures": info["graph_captures"], "work_items": info["work_items"],
-                    "seconds_batch_create": t_create, "clocks": clk.summary()}
+                    "seconds_batch_create": t_create, "clocks": clk.summary(),
+                    "roofline": {"bound": "fp32" if prec == ft.MIXED else "fp64", "achieved": tf, "peak": peak,
+                                 "unit": "TFLOP/s", "frac": tf / peak,
+                                 "flops_per_sample_mean": sum(f * k for f, k in zip(flops, n)) / sum(n),
+                                 "flops_source": sorted(set(flop_src))}}
         if prec == ft.MIXED:
             out[tag]["fp64_fallback_rate"] = sum(r["fp64_fallback"] for r in res) / sum(n)
             out["e2e_mixed"] = {"value": sum(n) / (t_plans + t_create + ms * 1e-3), "unit": UNIT,
@@ -268,6 +303,7 @@ def configs_section(args, ft, workloads, torch, flush):
             N = 1e9 mixed (plain FP64 on 1e8 of the same stream: the rate does not
             depend on N at these sizes)."""
     stream = torch.cuda.Stream()
+    fp32_peak, fp64_peak = ft.device_peaks()
     out = {}
     for name, inp, n_mixed, n_fp64 in (("K4", workloads.k4_euclidean(), 10 ** 7, 10 ** 7),
                                       ("cube", workloads.cube_propagator(), 10 ** 9, 10 ** 8)):
@@ -286,8 +322,14 @@ def configs_section(args, ft, workloads, torch, flush):
                     if step >= 1:
                         times.append(ev0.elapsed_time(ev1))
             ms = sum(times) / len(times)
+            flops, src = algorithmic_flops(plan.E, plan.V, plan.K, bool(plan.info["deformed"]))
+            tf = flops * n / (ms * 1e-3) / 1e12
+            peak = fp32_peak if prec == ft.MIXED else fp64_peak
             entry[tag] = {"value": n / (ms * 1e-3), "unit": UNIT, "ms_per_step": ms,
-                          "fp64_fallback_rate": res["fp64_fallback"] / n, "integral": res["integral"]}
+                          "fp64_fallback_rate": res["fp64_fallback"] / n, "integral": res["integral"],
+                          "roofline": {"bound": "fp32" if prec == ft.MIXED else "fp64", "achieved": tf, "peak": peak,
+                                       "unit": "TFLOP/s", "frac": tf / peak, "flops_per_sample": flops,
+                                       "flops_source": src}}
         entry["mixed_over_fp64"] = entry["mixed"]["value"] / entry["plain_fp64"]["value"]
         out[name] = entry
         plan.close()
@@ -488,7 +530,7 @@ def main():
         return
 
     fp32_peak, fp64_peak = ft.device_peaks()
-    flops = algorithmic_flops(plan.E, plan.V, plan.K, bool(plan.info["deformed"]))
+    flops, flops_src = algorithmic_flops(plan.E, plan.V, plan.K, bool(plan.info["deformed"]))
     launches = sum(r["kernel_launches"] for r in r_mixed)
     fallback = sum(r["fp64_fallback"] for r in r_mixed) / (N * len(r_mixed))
     acc0 = integral[0][0][1]
@@ -541,10 +583,13 @@ def main():
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
                      "hbm": hbm,
-                     "note": "algorithmic flops per sample %.0f (reference algorithm) x samples per launch / the "
-                             "sampling kernels' CUDA-event time (ft_sample + its FP64 pass, %.2f ms); peak = FP32 "
-                             "FMA issue rate measured live by an FMA-chain probe (FP64: %.2f TFLOP/s). Neither "
-                             "HBM nor tensor cores bound this path: see hbm" % (flops, kms, fp64_peak)},
+                     "flops_per_sample": flops,
+                     "note": "algorithmic flops per sample %.0f of the reference's loop, %s: the oracle's "
+                             "restatement run with an operation-counting scalar (profiles/flop_counts.txt) x samples "
+                             "per launch / the sampling kernels' CUDA-event time (ft_sample + its FP64 pass, %.2f ms); "
+                             "peak = FP32 FMA issue rate measured live by an FMA-chain probe (FP64: %.2f TFLOP/s). "
+                             "Neither HBM nor tensor cores bound this path: see hbm" % (flops, flops_src, kms,
+                                                                                         fp64_peak)},
         "e2e": {"value": N * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clocks,

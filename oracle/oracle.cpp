@@ -2,6 +2,7 @@
 // it is pinned).  Plain C++17, no third-party code; each block cites the reference
 // lines it follows.
 #include "oracle.hpp"
+#include "opcount.hpp"
 
 #include <algorithm>
 #include <array>
@@ -19,6 +20,31 @@
 namespace fto {
 
 using cd = std::complex<double>;
+
+// complex companion of a real type: std::complex<double> for double, cx for the
+// operation-counting scalar
+template <class Real> struct cplx_of { using type = std::complex<Real>; };
+template <> struct cplx_of<cnt> { using type = cx; };
+template <class Real> using cplx_t = typename cplx_of<Real>::type;
+
+// the sampling templates call these unqualified, so that the counting scalar's
+// overloads are found beside the standard ones
+using std::abs;
+using std::arg;
+using std::cos;
+using std::exp;
+using std::fabs;
+using std::isfinite;
+using std::log;
+using std::polar;
+using std::pow;
+using std::sin;
+
+op_counts& ops()
+{
+    static thread_local op_counts c;
+    return c;
+}
 
 // ---------------------------------------------------------------- random streams
 // srcs/random.hpp:32-66 (splitmix64 seeding) and :124-139 (xoshiro256+ step)
@@ -143,10 +169,11 @@ static double omega(const problem& p, double D, int L, uint64_t sub)
 }
 
 // srcs/laplacian.hpp:70-99 (n x n, n = C-1, row major)
-static std::vector<double> pgp_matrix(const problem& p, int C, const std::vector<int>& cmap)
+template <class Real = double>
+static std::vector<Real> pgp_matrix(const problem& p, int C, const std::vector<int>& cmap)
 {
     int n = C - 1;
-    std::vector<double> M((size_t)n * n, 0.0);
+    std::vector<Real> M((size_t)n * n, Real(0.0));
     for (int i = 0; i < p.V; i++)
         for (int j = 0; j < p.V; j++) {
             int v = cmap[i], w = cmap[j];
@@ -181,16 +208,17 @@ static std::vector<F> reduced_laplacian(const problem& p, uint64_t contracted, i
 // LDL^T with symmetric pivoting; the pivot order is the one a left-looking LDLT
 // that picks the largest remaining *original* diagonal entry produces (the rule
 // of the library used at srcs/feynman_integral.hpp:216).  Reads the lower triangle.
-struct ldlt {
+template <class Real>
+struct ldlt_t {
     int n = 0;
     std::vector<int> perm;        // position -> original index
-    std::vector<double> L, D;     // unit lower factor (row major), diagonal
-    std::vector<double> diag, y, col;
+    std::vector<Real> L, D;       // unit lower factor (row major), diagonal
+    std::vector<Real> diag, y, col;
 
-    ldlt() = default;
-    ldlt(const std::vector<double>& A, int n_) { compute(A, n_); }
+    ldlt_t() = default;
+    ldlt_t(const std::vector<Real>& A, int n_) { compute(A, n_); }
 
-    void compute(const std::vector<double>& A, int n_)
+    void compute(const std::vector<Real>& A, int n_)
     {
         n = n_;
         perm.resize(n);
@@ -200,7 +228,7 @@ struct ldlt {
         for (int k = 0; k < n; k++) {
             int best = k;
             for (int i = k + 1; i < n; i++)
-                if (std::fabs(diag[i]) > std::fabs(diag[best])) best = i;
+                if (fabs(diag[i]) > fabs(diag[best])) best = i;
             std::swap(diag[k], diag[best]);
             std::swap(perm[k], perm[best]);
         }
@@ -208,53 +236,53 @@ struct ldlt {
             int pi = perm[i], pj = perm[j];
             return pi >= pj ? A[pi * n + pj] : A[pj * n + pi];
         };
-        L.assign((size_t)n * n, 0.0);
-        D.assign(n, 0.0);
+        L.assign((size_t)n * n, Real(0.0));
+        D.assign(n, Real(0.0));
         for (int k = 0; k < n; k++) {
-            double d = a(k, k);
+            Real d = a(k, k);
             for (int j = 0; j < k; j++) d -= L[k * n + j] * L[k * n + j] * D[j];
             D[k] = d;
             L[k * n + k] = 1.0;
             for (int i = k + 1; i < n; i++) {
-                double s = a(i, k);
+                Real s = a(i, k);
                 for (int j = 0; j < k; j++) s -= L[i * n + j] * D[j] * L[k * n + j];
-                L[i * n + k] = (d != 0.0) ? s / d : 0.0;
+                L[i * n + k] = (d != 0.0) ? s / d : Real(0.0);
             }
         }
     }
 
     // x = A^{-1} b (x and b may not alias)
-    void solve_into(const double* b, double* x)
+    void solve_into(const Real* b, Real* x)
     {
         y.resize(n);
         for (int i = 0; i < n; i++) y[i] = b[perm[i]];
         for (int i = 0; i < n; i++)
             for (int j = 0; j < i; j++) y[i] -= L[i * n + j] * y[j];
         for (int i = 0; i < n; i++)
-            y[i] = std::fabs(D[i]) > std::numeric_limits<double>::min() ? y[i] / D[i] : 0.0;
+            y[i] = fabs(D[i]) > std::numeric_limits<double>::min() ? y[i] / D[i] : Real(0.0);
         for (int i = n - 1; i >= 0; i--)
             for (int j = i + 1; j < n; j++) y[i] -= L[j * n + i] * y[j];
         for (int i = 0; i < n; i++) x[perm[i]] = y[i];
     }
 
-    std::vector<double> solve(const std::vector<double>& b)
+    std::vector<Real> solve(const std::vector<Real>& b)
     {
-        std::vector<double> x(n);
+        std::vector<Real> x(n);
         solve_into(b.data(), x.data());
         return x;
     }
 
-    double det() const
+    Real det() const
     {
-        double p = 1.0;
-        for (double d : D) p *= d;
+        Real p = 1.0;
+        for (const Real& d : D) p *= d;
         return p;
     }
 
     // trace(A^{-1} B), B row major n x n
-    double trace_solve(const std::vector<double>& B)
+    Real trace_solve(const std::vector<Real>& B)
     {
-        double t = 0.0;
+        Real t = 0.0;
         col.resize(2 * n);
         for (int j = 0; j < n; j++) {
             for (int i = 0; i < n; i++) col[i] = B[i * n + j];
@@ -264,19 +292,19 @@ struct ldlt {
         return t;
     }
 };
+using ldlt = ldlt_t<double>;
 
 // LU with complete pivoting (largest modulus, first in column-major order), as used
 // at srcs/feynman_integral.hpp:305.
-struct full_piv_lu {
+template <class Real>
+struct full_piv_lu_t {
+    using C = cplx_t<Real>;
     int n = 0;
-    std::vector<cd> lu;
+    std::vector<C> lu;
     std::vector<int> rowp, colp;   // transpositions
     int ntransp = 0;
 
-    full_piv_lu() = default;
-    full_piv_lu(std::vector<cd> A, int n_) { compute(A, n_); }
-
-    void compute(const std::vector<cd>& A, int n_)
+    void compute(const std::vector<C>& A, int n_)
     {
         n = n_;
         lu = A;
@@ -285,10 +313,10 @@ struct full_piv_lu {
         ntransp = 0;
         for (int k = 0; k < n; k++) {
             int br = k, bc = k;
-            double best = -1.0;
+            Real best = -1.0;
             for (int c = k; c < n; c++)
                 for (int r = k; r < n; r++) {
-                    double s = std::abs(lu[r * n + c]);
+                    Real s = abs(lu[r * n + c]);
                     if (s > best) { best = s; br = r; bc = c; }
                 }
             rowp[k] = br;
@@ -311,14 +339,14 @@ struct full_piv_lu {
         }
     }
 
-    cd det() const
+    C det() const
     {
-        cd p = 1.0;
+        C p(1.0);
         for (int i = 0; i < n; i++) p *= lu[i * n + i];
         return (ntransp % 2) ? -p : p;
     }
 
-    std::vector<cd> solve(std::vector<cd> b) const
+    std::vector<C> solve(std::vector<C> b) const
     {
         for (int k = 0; k < n; k++) std::swap(b[k], b[rowp[k]]);
         for (int i = 0; i < n; i++)
@@ -334,14 +362,16 @@ struct full_piv_lu {
 
 // LU with partial pivoting (largest modulus in the column, first wins), as used at
 // srcs/feynman_integral.hpp:314-316; only the determinant is needed.
-static cd partial_piv_det(std::vector<cd>& lu, int n)
+template <class Real>
+static cplx_t<Real> partial_piv_det(std::vector<cplx_t<Real>>& lu, int n)
 {
+    using C = cplx_t<Real>;
     int ntransp = 0;
     for (int k = 0; k < n; k++) {
         int br = k;
-        double best = std::abs(lu[k * n + k]);
+        Real best = abs(lu[k * n + k]);
         for (int r = k + 1; r < n; r++) {
-            double s = std::abs(lu[r * n + k]);
+            Real s = abs(lu[r * n + k]);
             if (s > best) { best = s; br = r; }
         }
         if (best != 0.0) {
@@ -354,7 +384,7 @@ static cd partial_piv_det(std::vector<cd>& lu, int n)
         for (int r = k + 1; r < n; r++)
             for (int c = k + 1; c < n; c++) lu[r * n + c] -= lu[r * n + k] * lu[k * n + c];
     }
-    cd p = 1.0;
+    C p(1.0);
     for (int i = 0; i < n; i++) p *= lu[i * n + i];
     return (ntransp % 2) ? -p : p;
 }
@@ -635,57 +665,62 @@ prepared prepare(const problem& in)
 
 // ---------------------------------------------------------------- sector draw
 // srcs/tropical_sampling.hpp:468-564
-sector draw_sector(const prepared& pr, xoshiro& g)
+template <class Real>
+static sector draw_sector_t(const prepared& pr, xoshiro& g)
 {
     const int E = pr.p.E;
     sector s;
     s.X.assign(E, 0.0);
     uint64_t sub = (1ULL << E) - 1;
-    double JJr = pr.Jr[sub];
+    Real JJr = pr.Jr[sub];
     bool MM = pr.mm[sub];
     int oL = pr.L[sub];
-    double G = 0.0, F = 1.0, XX = 1.0;
+    Real G = 0.0, F = 1.0, XX = 1.0;
     for (int j = 0;; j++) {
         // get_random_cut: first edge (ascending) whose running sum exceeds u*JJr,
         // else the last edge visited
-        double R = g.uniform() * JJr;
-        double T = 0.0;
+        const Real u = Real((double)(g.next() >> 11)) * (1.0 / 9007199254740992.0);
+        Real R = u * JJr;
+        Real T = 0.0;
         int e = -1;
         for (int c = 0; c < E; c++) {
             if (!((sub >> c) & 1)) continue;
             uint64_t t = sub & ~(1ULL << c);
-            T += pr.Jr[t] / pr.r[t];
+            T += Real(pr.Jr[t]) / pr.r[t];
             e = c;
             if (T > R) break;
         }
         sub &= ~(1ULL << e);
         JJr = pr.Jr[sub];
-        double r = pr.r[sub];
+        Real r = pr.r[sub];
         bool mm = pr.mm[sub];
         int L = pr.L[sub];
         s.order.push_back(e);
         if (MM && !mm) G = XX;
         MM = mm;
-        s.X[e] = XX;
+        s.X[e] = (double)XX;
         if (L < oL) {
             F *= XX;
             oL = L;
         }
         if (j >= E - 1) break;
-        double U = g.uniform();
-        XX *= std::pow(1. - U, 1. / r);
+        const Real U = Real((double)(g.next() >> 11)) * (1.0 / 9007199254740992.0);
+        XX *= pow(1. - U, 1. / r);
     }
-    s.psi_tr = F;
-    s.xi_tr = G * F;
+    s.psi_tr = (double)F;
+    s.xi_tr = (double)(G * F);
     return s;
 }
 
+sector draw_sector(const prepared& pr, xoshiro& g) { return draw_sector_t<double>(pr, g); }
+
 // ---------------------------------------------------------------- integrand
 // srcs/laplacian.hpp:102-215 for an empty contracted subgraph
+template <class Real>
 static void pphi_derivatives(const problem& p, int C, const std::vector<int>& cmap,
-                             const std::vector<double>& xinv, const std::vector<double>& xinv2,
-                             const std::vector<double>& Ginv, const std::vector<double>& M,
-                             std::vector<double>& d, std::vector<double>& dd)
+                             const std::vector<Real>& xinv, const std::vector<Real>& xinv2,
+                             const std::vector<Real>& Ginv, const std::vector<Real>& M,
+                             std::vector<Real>& d, std::vector<Real>& dd)
 {
     const int E = p.E, n = C - 1;
     auto LP = [&](int i, int j) { return M[i * n + j]; };
@@ -693,7 +728,7 @@ static void pphi_derivatives(const problem& p, int C, const std::vector<int>& cm
     for (int a = 0; a < E; a++) {
         int ka = cmap[p.k[a]], la = cmap[p.l[a]];
         if (la > ka) std::swap(la, ka);
-        double s, t;
+        Real s, t;
         if (ka == C - 1) {
             s = LP(la, la);
             t = LI(la, la);
@@ -701,14 +736,14 @@ static void pphi_derivatives(const problem& p, int C, const std::vector<int>& cm
             s = LP(ka, ka) + LP(la, la) - 2. * LP(ka, la);
             t = LI(ka, ka) + LI(la, la) - 2. * LI(ka, la);
         }
-        double xa = xinv2[a];
-        double xas = xa * s;
+        Real xa = xinv2[a];
+        Real xas = xa * s;
         d[a] = -xas;
         dd[a * E + a] = 2. * xas * (xinv[a] - xa * t);
         for (int b = a + 1; b < E; b++) {
             int kb = cmap[p.k[b]], lb = cmap[p.l[b]];
             if (lb > kb) std::swap(lb, kb);
-            double s2, t2;
+            Real s2, t2;
             if (kb == C - 1) {
                 if (ka == C - 1) {
                     s2 = LP(la, lb);
@@ -726,34 +761,37 @@ static void pphi_derivatives(const problem& p, int C, const std::vector<int>& cm
                     t2 = LI(ka, kb) + LI(la, lb) - LI(ka, lb) - LI(la, kb);
                 }
             }
-            double xb = xinv2[b];
+            Real xb = xinv2[b];
             dd[a * E + b] = dd[b * E + a] = -2. * xa * xb * s2 * t2;
         }
     }
 }
 
-static cd cpow(cd x, double y)
+template <class C>
+static C cpow(const C& x, double y)
 {
     // principal branch, as the standard complex power with a real exponent
-    double lr = std::log(std::abs(x)), th = std::arg(x);
-    return std::polar(std::exp(y * lr), y * th);
+    const auto lr = log(abs(x)), th = arg(x);
+    return polar(exp(y * lr), y * th);
 }
 
-// srcs/feynman_integral.hpp:162-362
-sample_value evaluate(const prepared& pr, const sector& sec)
+// srcs/feynman_integral.hpp:162-362.  Writes the K eps-order values into `out`;
+// returns false when the sample is dropped.
+template <class Real>
+static bool evaluate_t(const prepared& pr, const sector& sec, std::vector<cplx_t<Real>>& out)
 {
+    using C = cplx_t<Real>;
     const problem& p = pr.p;
     const int E = p.E, V = p.V, n = V - 1, K = p.K;
     const double D = p.D, W = pr.W;
     const int L = pr.loops;
-    sample_value out;
-    out.R.assign(K, cd(0, 0));
+    out.assign(K, C(0.0));
 
-    std::vector<double> X = sec.X;
-    double psi_tr = sec.psi_tr, xi_tr = sec.xi_tr;
+    std::vector<Real> X(sec.X.begin(), sec.X.end());
+    const Real psi_tr = sec.psi_tr, xi_tr = sec.xi_tr;
 
     // vertex with the smallest incident X becomes the deleted row/column
-    std::vector<double> XV(V, 0.0);
+    std::vector<Real> XV(V, Real(0.0));
     for (int j = 0; j < E; j++) {
         XV[p.k[j]] += X[j];
         XV[p.l[j]] += X[j];
@@ -765,138 +803,137 @@ sample_value evaluate(const prepared& pr, const sector& sec)
     for (int i = 0; i < V; i++) cmap[i] = i < minV ? i : (i > minV ? i - 1 : V - 1);
 
     // normalise so that psi_tr^(-D/2) (psi_tr/xi_tr)^W = 1
-    double tgt = std::pow(psi_tr, -D / 2.) * std::pow(psi_tr / xi_tr, W);
-    double scale = std::pow(tgt, 1. / (D / 2. * L + W));
-    for (double& x : X) x *= scale;
-    std::vector<double> Xinv(E);
+    Real tgt = pow(psi_tr, -D / 2.) * pow(psi_tr / xi_tr, W);
+    Real scale = pow(tgt, 1. / (D / 2. * L + W));
+    for (Real& x : X) x *= scale;
+    std::vector<Real> Xinv(E);
     for (int j = 0; j < E; j++) Xinv[j] = 1.0 / X[j];
 
-    auto La = reduced_laplacian<double>(p, 0, V, cmap, Xinv);
-    static thread_local ldlt f;
+    auto La = reduced_laplacian<Real>(p, 0, V, cmap, Xinv);
+    static thread_local ldlt_t<Real> f;
     f.compute(La, n);
-    double Xprod = 1.0;
-    for (double x : X) Xprod *= x;
+    Real Xprod = 1.0;
+    for (const Real& x : X) Xprod *= x;
 
     if (pr.def_ref == 0. || (pr.W_zero && K == 1)) {
-        double psi = f.det() * Xprod;
-        double R = pr.IGtr * std::pow(psi, -D / 2.);
-        if (!std::isfinite(R)) {
-            out.dropped = true;
-            return out;
-        }
+        Real psi = f.det() * Xprod;
+        Real R = pr.IGtr * pow(psi, -D / 2.);
+        if (!isfinite(R)) return false;
         if (pr.W_zero && K == 1) {
-            out.R[0] = R;
-            return out;
+            out[0] = C(R);
+            return true;
         }
-        auto PGP = pgp_matrix(p, V, cmap);
-        double pphi = -f.trace_solve(PGP);
-        double pxi = pphi;
+        auto PGP = pgp_matrix<Real>(p, V, cmap);
+        Real pphi = -f.trace_solve(PGP);
+        Real pxi = pphi;
         for (int j = 0; j < E; j++) pxi += p.m2[j] * X[j];
-        R *= std::pow(pxi, -W);
-        if (!std::isfinite(R)) {
-            out.dropped = true;
-            return out;
-        }
-        out.R[0] = R;
+        R *= pow(pxi, -W);
+        if (!isfinite(R)) return false;
+        out[0] = C(R);
         if (K > 1) {
-            double eps_fac = std::log(psi) - L * std::log(pxi);
+            Real eps_fac = log(psi) - L * log(pxi);
             for (int j = 1; j < K; j++) {
                 R *= eps_fac / (double)j;
-                out.R[j] = R;
+                out[j] = C(R);
             }
         }
-        return out;
+        return true;
     }
 
     // deformed (Minkowski) branch
-    auto PGP = pgp_matrix(p, V, cmap);
-    static thread_local std::vector<double> Ginv;
-    Ginv.assign((size_t)n * n, 0.0);
+    auto PGP = pgp_matrix<Real>(p, V, cmap);
+    static thread_local std::vector<Real> Ginv;
+    Ginv.assign((size_t)n * n, Real(0.0));
     {
-        static thread_local std::vector<double> col;
-        col.assign(2 * n, 0.0);
+        static thread_local std::vector<Real> col;
+        col.assign(2 * n, Real(0.0));
         for (int j = 0; j < n; j++) {
             for (int i = 0; i < n; i++) col[i] = (i == j) ? 1.0 : 0.0;
             f.solve_into(col.data(), col.data() + n);
             for (int i = 0; i < n; i++) Ginv[i * n + j] = col[n + i];
         }
     }
-    static thread_local std::vector<double> T1, M;
-    T1.assign((size_t)n * n, 0.0);
-    M.assign((size_t)n * n, 0.0);
+    static thread_local std::vector<Real> T1, M;
+    T1.assign((size_t)n * n, Real(0.0));
+    M.assign((size_t)n * n, Real(0.0));
     for (int i = 0; i < n; i++)
         for (int j = 0; j < n; j++) {
-            double s = 0;
+            Real s = 0;
             for (int k = 0; k < n; k++) s += Ginv[i * n + k] * PGP[k * n + j];
             T1[i * n + j] = s;
         }
     for (int i = 0; i < n; i++)
         for (int j = 0; j < n; j++) {
-            double s = 0;
+            Real s = 0;
             for (int k = 0; k < n; k++) s += T1[i * n + k] * Ginv[j * n + k];
             M[i * n + j] = s;
         }
-    static thread_local std::vector<double> Xinv2;
-    Xinv2.assign(E, 0.0);
+    static thread_local std::vector<Real> Xinv2;
+    Xinv2.assign(E, Real(0.0));
     for (int j = 0; j < E; j++) Xinv2[j] = Xinv[j] * Xinv[j];
-    static thread_local std::vector<double> d, dd;
-    d.assign(E, 0.0);
-    dd.assign((size_t)E * E, 0.0);
-    pphi_derivatives(p, V, cmap, Xinv, Xinv2, Ginv, M, d, dd);
+    static thread_local std::vector<Real> d, dd;
+    d.assign(E, Real(0.0));
+    dd.assign((size_t)E * E, Real(0.0));
+    pphi_derivatives<Real>(p, V, cmap, Xinv, Xinv2, Ginv, M, d, dd);
     for (int j = 0; j < E; j++) d[j] = (d[j] + p.m2[j]) * pr.def_ref;
 
-    static thread_local std::vector<cd> cX, cXinv;
-    cX.assign(E, cd(0, 0));
-    cXinv.assign(E, cd(0, 0));
+    static thread_local std::vector<C> cX, cXinv;
+    cX.assign(E, C(0.0));
+    cXinv.assign(E, C(0.0));
     for (int j = 0; j < E; j++) {
-        cX[j] = X[j] * cd(std::cos(d[j]), std::sin(d[j]));
+        cX[j] = X[j] * C(cos(d[j]), sin(d[j]));
         cXinv[j] = 1.0 / cX[j];
     }
-    auto cLa = reduced_laplacian<cd>(p, 0, V, cmap, cXinv);
+    auto cLa = reduced_laplacian<C>(p, 0, V, cmap, cXinv);
     for (int k = 0; k < n; k++)
         for (int l = k + 1; l < n; l++) cLa[k * n + l] = cLa[l * n + k];
-    static thread_local full_piv_lu lu;
+    static thread_local full_piv_lu_t<Real> lu;
     lu.compute(cLa, n);
-    cd cXprod = 1.0;
+    C cXprod(1.0);
     for (auto& c : cX) cXprod *= c;
-    cd cPsi = cXprod * lu.det();
-    cd cR = pr.IGtr * cpow(cPsi, -D / 2.);
+    C cPsi = cXprod * lu.det();
+    C cR = pr.IGtr * cpow(cPsi, -D / 2.);
 
-    static thread_local std::vector<cd> J;
-    J.assign((size_t)E * E, cd(0, 0));
+    static thread_local std::vector<C> J;
+    J.assign((size_t)E * E, C(0.0));
     for (int a = 0; a < E; a++)
         for (int b = 0; b < E; b++)
-            J[a * E + b] = cd(0., pr.def_ref) * dd[a * E + b] * X[b] + (a == b ? 1.0 : 0.0);
-    cd det_jac = partial_piv_det(J, E);
-    double x_nu = 0;
+            J[a * E + b] = C(0., pr.def_ref) * dd[a * E + b] * X[b] + (a == b ? 1.0 : 0.0);
+    C det_jac = partial_piv_det<Real>(J, E);
+    Real x_nu = 0;
     for (int j = 0; j < E; j++) x_nu += p.nu[j] * d[j];
-    cR *= det_jac * cd(std::cos(x_nu), std::sin(x_nu));
+    cR *= det_jac * C(cos(x_nu), sin(x_nu));
 
-    cd tr = 0;
+    C tr(0.0);
     {
-        std::vector<cd> col(n);
+        std::vector<C> col(n);
         for (int j = 0; j < n; j++) {
-            for (int i = 0; i < n; i++) col[i] = PGP[i * n + j];
+            for (int i = 0; i < n; i++) col[i] = C(PGP[i * n + j]);
             tr += lu.solve(col)[j];
         }
     }
-    cd cPPhi = -tr;
-    cd cPXi = cPPhi;
+    C cPPhi = -tr;
+    C cPXi = cPPhi;
     for (int j = 0; j < E; j++) cPXi += p.m2[j] * cX[j];
     cR *= cpow(cPXi, -W);
-    if (!std::isfinite(cR.real()) || !std::isfinite(cR.imag())) {
-        out.dropped = true;
-        return out;
-    }
-    out.R[0] = cR;
+    if (!isfinite(cR.real()) || !isfinite(cR.imag())) return false;
+    out[0] = cR;
     if (K > 1) {
-        cd eps_fac = std::log(cPsi) - (double)L * std::log(cPXi);
+        C eps_fac = log(cPsi) - (double)L * log(cPXi);
         for (int j = 1; j < K; j++) {
             cR *= eps_fac / (double)j;
-            out.R[j] = cR;
+            out[j] = cR;
         }
     }
-    return out;
+    return true;
+}
+
+sample_value evaluate(const prepared& pr, const sector& sec)
+{
+    sample_value v;
+    v.dropped = !evaluate_t<double>(pr, sec, v.R);
+    if (v.dropped) v.R.assign(pr.p.K, cd(0, 0));
+    return v;
 }
 
 // ---------------------------------------------------------------- statistics
@@ -1135,6 +1172,39 @@ int fto_integrate(void* h, uint64_t N, uint64_t seed, int threads, double* out, 
             counts[0] = est.kept;
             counts[1] = est.dropped;
         }
+        return 0;
+    } catch (std::exception& e) {
+        g_err = e.what();
+        return 1;
+    }
+}
+
+// Operation counts of samples first..first+count-1 of stream `seed`, run through the
+// same restatement with the counting scalar.  out[7]: adds, muls, divs, sqrts,
+// transcendentals, comparisons (summed over the samples) and the dropped count;
+// R (optional, count x K complex) receives the counted run's values.
+int fto_count_ops(void* h, uint64_t seed, uint64_t first, uint64_t count, double* out, double* R)
+{
+    try {
+        auto* pr = (fto::prepared*)h;
+        const int E = pr->p.E, K = pr->p.K;
+        fto::xoshiro g(seed);
+        fto::skip(g, first * (uint64_t)(2 * E - 1));
+        fto::op_counts& c = fto::ops();
+        c = fto::op_counts();
+        double dropped = 0;
+        std::vector<fto::cx> v;
+        for (uint64_t i = 0; i < count; i++) {
+            fto::sector s = fto::draw_sector_t<fto::cnt>(*pr, g);
+            const bool kept = fto::evaluate_t<fto::cnt>(*pr, s, v);
+            if (!kept) dropped++;
+            for (int j = 0; j < K && R; j++) {
+                R[(i * K + j) * 2] = kept ? v[j].re.v : 0.0;
+                R[(i * K + j) * 2 + 1] = kept ? v[j].im.v : 0.0;
+            }
+        }
+        const double o[7] = {c.add, c.mul, c.div, c.sqrt, c.trans, c.cmp, dropped};
+        std::memcpy(out, o, sizeof o);
         return 0;
     } catch (std::exception& e) {
         g_err = e.what();

@@ -41,6 +41,8 @@ def lib(fast=False):
             L.fto_integrate.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
                                         ctypes.c_void_p, ctypes.c_void_p]
             L.fto_skip.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_void_p]
+            L.fto_count_ops.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                        ctypes.c_void_p, ctypes.c_void_p]
             _libs[name] = L
         return _libs[name]
 
@@ -101,6 +103,21 @@ class Prepared:
             raise OracleError(self.L.fto_last_error().decode())
         return {"order": order, "X": X, "psi_tr": psi, "xi_tr": xi, "R": R[..., 0] + 1j * R[..., 1],
                 "dropped": dropped.astype(bool)}
+
+    def count_ops(self, seed, first, count, values=False):
+        """Floating-point operations of samples first..first+count-1, counted by running
+        the restatement with the counting scalar (oracle/opcount.hpp).  Returns a dict of
+        totals (add, mul, div, sqrt, trans, cmp, dropped) and, with values=True, the
+        counted run's per-sample values (count x K complex)."""
+        out = np.zeros(7)
+        R = np.zeros((count, self.K, 2)) if values else None
+        rc = self.L.fto_count_ops(self.h, seed, first, count, _ptr(out), _ptr(R) if values else None)
+        if rc:
+            raise OracleError(self.L.fto_last_error().decode())
+        d = dict(zip(("add", "mul", "div", "sqrt", "trans", "cmp", "dropped"), out.tolist()))
+        if values:
+            d["R"] = R[..., 0] + 1j * R[..., 1]
+        return d
 
     def integrate(self, N, seed=0, threads=1):
         out = np.zeros((self.K, 4))
