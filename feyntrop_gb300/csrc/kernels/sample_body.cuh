@@ -296,6 +296,25 @@ struct elim {
         return s;
     }
 
+    // q^T L^{-1} q as quad(), adding sum_i |y_i|^2 / |d_i| (the magnitude of its terms) to mag
+    template <class Q>
+    __device__ __forceinline__ F quad_mag(const Q* q, R& mag) const
+    {
+        F y[FT_N];
+        F s = F{};
+#pragma unroll
+        for (int i = 0; i < FT_N; i++) {
+            F yi = from_real((R)q[i]);
+#pragma unroll
+            for (int k = 0; k < i; k++) yi = yi + a[k][i] * y[k];
+            y[i] = yi;
+            const F t = yi * yi * inv_of(d[i]);
+            s = s + t;
+            mag += mag_of(t);
+        }
+        return s;
+    }
+
     static __device__ __forceinline__ R mag_of(R x) { return fabs(x); }
     static __device__ __forceinline__ R mag_of(cx<R> x) { return fabs(x.re) + fabs(x.im); }
     static __device__ __forceinline__ R inv_of(R x) { return rcp_(x); }
@@ -1051,6 +1070,15 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
     cx<double> cPXi = cpphi;
 #pragma unroll
     for (int e = 0; e < FT_E; e++) cPXi = cPXi + prm[P_M2 + e] * cX[e];
+    FT_DBG(50, log2(hypot(detJ.re, detJ.im)));
+    FT_DBG(51, atan2(detJ.im, detJ.re));
+    FT_DBG(52, atan2(cPsi.im, cPsi.re));
+    FT_DBG(54, atan2(cPXi.im, cPXi.re));
+    FT_DBG(55, xnu);
+    FT_DBG(56, cpphi.re);
+    FT_DBG(57, cpphi.im);
+    FT_DBG(58, cPXi.re);
+    FT_DBG(59, cPXi.im);
     cR = cR * cpow_(cPXi, -W);
     if (!cfinite(cR)) return false;
     out[0] = cR;
@@ -1335,11 +1363,14 @@ static __device__ __forceinline__ f2 f2_neg(f2 a) { return f2_make(-a.hi, -a.lo)
 #ifndef DET_CANCEL
 #define DET_CANCEL 400.0f
 #endif
-// largest accepted W (sum |terms of V|) / (|V| pivot growth) in the deformed integrand:
-// V^(-W) carries the FP32 error of the complex solves (grown by 1 / pivot growth),
-// amplified by the cancellation in V
+// largest accepted W qmag / |V| in the deformed integrand, qmag the magnitude of every
+// term summed into V (the forward substitutions' y_i^2 / d_i weighted by |sigma_r|, and
+// the mass terms): V^(-W) carries their FP32 rounding, amplified by the cancellation in
+// V.  At 120 the mixed form's samples stay within about 1.4e-5 of FP64 on random
+// box-pentagon kinematics with ~1 % handed off (the pivot-growth bound it replaces
+// let 0.02-0.03 % of the samples exceed 1e-5 at 0.7 %)
 #ifndef V_AMPLIFY
-#define V_AMPLIFY 400.0f
+#define V_AMPLIFY 120.0f
 #endif
 #define RLN2_HI 1.44269502162933349609375f
 #define RLN2_LO 1.925963033500011e-8f
@@ -1539,9 +1570,12 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     // phi/psi of the deformed point and the deformed V
     cx<float> cpphi = cmk(0.0f, 0.0f);
     float mag = 0.0f;
+    float qmag = 0.0f;   // magnitude of the terms summed into V, through the eliminations
 #pragma unroll
     for (int r = 0; r < FT_RANK; r++) {
-        const cx<float> v = pf[P_SIG + r] * CL.quad(pf + P_Q + r * FT_N);
+        float qm = 0.0f;
+        const cx<float> v = pf[P_SIG + r] * CL.quad_mag(pf + P_Q + r * FT_N, qm);
+        qmag += fabsf(pf[P_SIG + r]) * qm;
         cpphi = cpphi - v;
         mag += cabs_(v);
     }
@@ -1551,21 +1585,29 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
         cV = cV + pf[P_M2 + e] * cX[e];
         mag += pf[P_M2 + e] * X[e];
     }
+    qmag += mag;
     const float vabs = cabs_(cV);
     FT_DBG(20, cV.re);
     FT_DBG(21, cV.im);
     FT_DBG(22, cpphi.re);
     FT_DBG(23, cpphi.im);
     // V cancels near thresholds: its FP32 error is ~ 1e-7 * mag / |V|, so samples where
-    // |V| < V_CANCEL * mag go to the FP64 pass
-    if (!(vabs > V_CANCEL * mag) || !(W * mag < V_AMPLIFY * growth * vabs)) {
+    // |V| < V_CANCEL * mag go to the FP64 pass.  The rounding inside the eliminations
+    // is bounded by the magnitudes of the terms they sum (qmag: sum_r |sigma_r|
+    // sum_i |y_i^2 / d_i| of the forward substitutions, plus the mass terms); V^-W
+    // turns it into a relative error of about 1e-7 W qmag / |V|.
+    if (!(vabs > V_CANCEL * mag) || !(W * qmag < V_AMPLIFY * vabs)) {
         need64 = true;
         return false;
     }
+
     mexp mv = mx_one();
     mx_mul(mv, vabs);
     const float av = m_atan2(cV.im, cV.re);
     edge |= fabsf(av) > 3.14158265f;
+    FT_DBG(32, av);
+    FT_DBG(34, W * qmag / vabs);
+    FT_DBG(33, xnu.hi + xnu.lo);
     // det(I + i kappa X^1/2 H X^1/2)
     cx<float> J[FT_E][FT_E];
     float sx[FT_E];
