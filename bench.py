@@ -73,6 +73,14 @@ def _flop_table():
 
 
 FLOP_TABLE = _flop_table()
+_PEAKS = []
+
+
+def device_peaks(ft):
+    """(FP32, FP64) FMA rates of this GPU, probed once per process (outside every timed region)."""
+    if not _PEAKS:
+        _PEAKS.append(ft.device_peaks())
+    return _PEAKS[0]
 
 
 def algorithmic_flops(E, V, K, deformed):
@@ -217,7 +225,7 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
     plans = ft.create_plans(inputs)
     t_plans = time.perf_counter() - t0
     Ns = [x["N"] for x in inputs]
-    fp32_peak, fp64_peak = ft.device_peaks()
+    fp32_peak, fp64_peak = device_peaks(ft)
     fl = [algorithmic_flops(p.E, p.V, p.K, bool(p.info["deformed"])) for p in plans]
     flops, flop_src = [f for f, _ in fl], [s_ for _, s_ in fl]
     stream = torch.cuda.Stream()
@@ -303,7 +311,7 @@ def configs_section(args, ft, workloads, torch, flush):
             N = 1e9 mixed (plain FP64 on 1e8 of the same stream: the rate does not
             depend on N at these sizes)."""
     stream = torch.cuda.Stream()
-    fp32_peak, fp64_peak = ft.device_peaks()
+    fp32_peak, fp64_peak = device_peaks(ft)
     out = {}
     for name, inp, n_mixed, n_fp64 in (("K4", workloads.k4_euclidean(), 10 ** 7, 10 ** 7),
                                       ("cube", workloads.cube_propagator(), 10 ** 9, 10 ** 8)):
@@ -529,7 +537,7 @@ def main():
             dist.destroy_process_group()
         return
 
-    fp32_peak, fp64_peak = ft.device_peaks()
+    fp32_peak, fp64_peak = device_peaks(ft)
     flops, flops_src = algorithmic_flops(plan.E, plan.V, plan.K, bool(plan.info["deformed"]))
     launches = sum(r["kernel_launches"] for r in r_mixed)
     fallback = sum(r["fp64_fallback"] for r in r_mixed) / (N * len(r_mixed))
