@@ -187,20 +187,31 @@ void build(ft_batch& b)
         g.rank = std::max(g.rank, (int)pl->sigma.size());
     }
     const device_state& ds = dev_state();
-    size_t hdr = 0, inst = 0, prep = 0;
+    // every class's kernels (and, mixed, the FP64 ones its hand-offs run on), compiled
+    // concurrently before they are loaded one by one
+    std::vector<ft::kernel_key> keys, keys64;
     for (ft_batch::group& g : b.groups) {
+        g.key.rank = g.rank;
+        g.key.batch = 1;
+        keys.push_back(g.key);
+        ft::kernel_key k64 = b.plans[g.members[0]]->key(0, 0);
+        k64.rank = g.rank;
+        k64.batch = 1;
+        keys64.push_back(k64);
+    }
+    {
+        std::vector<ft::kernel_key> all = keys;
+        if (prec) all.insert(all.end(), keys64.begin(), keys64.end());
+        ft::precompile_all(all);
+    }
+    size_t hdr = 0, inst = 0, prep = 0;
+    for (size_t gi = 0; gi < b.groups.size(); gi++) {
+        ft_batch::group& g = b.groups[gi];
         const ft_plan& p0 = *b.plans[g.members[0]];
         g.K = p0.P.K;
         g.draws = 2 * p0.P.E - 1;
-        g.key.rank = g.rank;
-        g.key.batch = 1;
         g.ks = &ft::get_kernels(g.key);
-        if (prec) {
-            ft::kernel_key k64 = p0.key(0, 0);
-            k64.rank = g.rank;
-            k64.batch = 1;
-            g.k64 = &ft::get_kernels(k64);
-        }
+        if (prec) g.k64 = &ft::get_kernels(keys64[gi]);
         const ft::launch_shape tuned = ft::choose_shape(g.key);
         g.chunk = ft::chunk_override()
                       ? ft::chunk_override()

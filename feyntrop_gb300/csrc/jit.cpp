@@ -5,6 +5,8 @@
 #include <nvrtc.h>
 #include <sys/stat.h>
 
+#include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -14,6 +16,8 @@
 #include <mutex>
 #include <sstream>
 #include <stdexcept>
+#include <thread>
+#include <vector>
 
 extern const char* ft_sample_body_source;   // generated at build time from kernels/sample_body.cuh
 
@@ -186,6 +190,31 @@ void precompile(const kernel_key& key)
     cubin_for(key, &s);
 }
 
+void precompile_all(const std::vector<kernel_key>& keys)
+{
+    if (keys.size() < 2) {
+        for (const kernel_key& k : keys) precompile(k);
+        return;
+    }
+    // at most 8 at a time: a compile of the larger kernels takes about a gigabyte
+    const unsigned hw = std::max(1u, std::min(8u, std::thread::hardware_concurrency()));
+    const size_t nthreads = std::min<size_t>(keys.size(), hw);
+    std::atomic<size_t> next{0};
+    std::vector<std::exception_ptr> errs(nthreads);
+    std::vector<std::thread> pool;
+    for (size_t t = 0; t < nthreads; t++)
+        pool.emplace_back([&, t] {
+            try {
+                for (size_t i; (i = next++) < keys.size();) precompile(keys[i]);
+            } catch (...) {
+                errs[t] = std::current_exception();
+            }
+        });
+    for (auto& th : pool) th.join();
+    for (auto& e : errs)
+        if (e) std::rethrow_exception(e);
+}
+
 // Driver entry points are fetched through the runtime (no link-time dependency on
 // the driver library, so the library also loads on machines without a GPU).
 driver_api& drv()
@@ -247,16 +276,22 @@ const kernel_set& get_kernels(const kernel_key& key)
     auto& loaded = g_loaded;
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) throw std::runtime_error("no CUDA device");
-    std::lock_guard<std::mutex> lock(mu);
     auto k = std::make_pair(dev, key_string(key));
-    auto it = loaded.find(k);
-    if (it != loaded.end()) return it->second;
-
-    cudaFree(0);   // make the runtime's primary context current for the driver calls
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = loaded.find(k);
+        if (it != loaded.end()) return it->second;
+    }
+    // compile (or read the disk cache) outside the lock, so that threads loading
+    // different kernels compile them concurrently
     kernel_set ks;
     ks.block = key.block;
     ks.variant = key.variant;
     const std::string cubin = cubin_for(key, &ks.compile_seconds);
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = loaded.find(k);
+    if (it != loaded.end()) return it->second;   // another thread loaded it meanwhile
+    cudaFree(0);   // make the runtime's primary context current for the driver calls
     check(drv().ModuleLoadData(&ks.module, cubin.data()), "cuModuleLoadData");
     const char* sname = key.batch ? "ft_sample_batch" : "ft_sample";
     const char* qname = key.batch ? "ft_sample_queue_batch" : "ft_sample_queue";

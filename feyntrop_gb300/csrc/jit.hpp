@@ -74,5 +74,7 @@ size_t compile_only(const kernel_key& key, std::string* log = nullptr);
 
 // compile into the on-disk cache unless it is there already
 void precompile(const kernel_key& key);
+// the cubins of several keys, compiled concurrently on the host's threads
+void precompile_all(const std::vector<kernel_key>& keys);
 
 }  // namespace ft

@@ -335,6 +335,7 @@ run_out run(ft_plan& pl, const ft_run_options& o, cudaStream_t st, const records
 {
     const int prec = o.precision == FT_PRECISION_MIXED ? 1 : 0;
     const int record = rec ? 1 : 0;
+    if (prec && !ft::find_kernels(pl.key(prec, record))) ft::precompile_all({pl.key(prec, record), pl.key(0, record)});
     const ft::kernel_set& ks = ft::get_kernels(pl.key(prec, record));
     const ft::kernel_set* k64 = prec ? &ft::get_kernels(pl.key(0, record)) : nullptr;
     const unsigned long long N = o.num_samples;
@@ -633,16 +634,18 @@ int ft_precompile(const ft_problem* pb, int32_t precision, double* seconds)
         auto t0 = std::chrono::steady_clock::now();
         const int prec = precision & 0xff;
         const bool batch = (precision & FT_PRECOMPILE_BATCH) != 0;
+        std::vector<ft::kernel_key> keys;
         for (int bt = 0; bt <= (batch ? 1 : 0); bt++) {
             ft::kernel_key k = pl.key(0, 0);
             k.batch = bt;
-            ft::precompile(k);
+            keys.push_back(k);
             if (prec == FT_PRECISION_MIXED) {
                 k = pl.key(1, 0);
                 k.batch = bt;
-                ft::precompile(k);
+                keys.push_back(k);
             }
         }
+        ft::precompile_all(keys);
         if (seconds) *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         return FT_OK;
     } catch (...) {
