@@ -814,6 +814,17 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
             for (int var : {v | 4, v})
                 for (int bm : {256, 128, 512}) add(bm, bm == 128 ? 2 : 1, var);
         }
+        {
+            // every candidate's kernels compiled concurrently before the timing
+            std::vector<ft::kernel_key> keys;
+            for (const ft::launch_shape& c : cands) {
+                ft::kernel_key k = pl->key(prec, 0);
+                ft::apply_shape(k, c);
+                keys.push_back(k);
+            }
+            if (prec == 1) keys.push_back(pl->key(0, 0));
+            ft::precompile_all(keys);
+        }
         ft_run_options o{};
         o.num_samples = samples;
         o.precision = precision;
@@ -858,9 +869,12 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
         best.rate = best_rate;
         ft::record_shape(pl->key(prec, 0), best);
         // the batch work item (samples per thread) of the class, under the chosen shape:
-        // a batch of this one integral per candidate
+        // a batch of this one integral per candidate, with enough samples that even the
+        // largest item leaves every SM four items
         double best_batch = -1;
         unsigned long long best_chunk = 0;
+        const uint64_t bsamples =
+            std::max<uint64_t>(samples, (uint64_t)dev_state().sms * (uint64_t)pl->key(prec, 0).block * 256ull * 4ull);
         for (unsigned long long c : {32ull, 64ull, 128ull, 256ull}) {
             ft::set_chunk_override(c);
             ft_batch* b = nullptr;
@@ -877,12 +891,13 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
             double rate = 0;
             for (int rep = 0; rep < 3 && rc == FT_OK; rep++) {
                 ft_run_options bo = o;
+                bo.num_samples = bsamples;
                 bo.seed = (uint64_t)rep;
                 bo.stream = nullptr;
                 rc = ft_batch_run(b, &bo, &r);
                 ft_batch_info bi{};
                 ft_batch_get_info(b, &bi);
-                if (rep > 0 && bi.kernel_ms > 0) rate = std::max(rate, (double)samples / (bi.kernel_ms * 1e-3));
+                if (rep > 0 && bi.kernel_ms > 0) rate = std::max(rate, (double)bsamples / (bi.kernel_ms * 1e-3));
             }
             ft_batch_destroy(b);
             if (rc != FT_OK) throw std::runtime_error(std::string("ft_autotune: batch run: ") + g_error);

@@ -203,9 +203,11 @@ int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds)
  * orders, regime, precision) under candidate launch shapes (threads per block, blocks
  * per SM given to the register allocator, code-size variants), `samples` samples per
  * trial, then the batch work-item size (samples per thread: 32 .. 256) under the chosen
- * shape, and records both in the tuning table (in memory and in tuning.json
- * beside the kernel cache), which every later plan and batch of the class uses.
- * Compiles each candidate on first use. */
+ * shape (batches of this integral with at least 1024 samples per thread of the GPU, so
+ * that the largest item still leaves every SM several), and records both in the tuning
+ * table (in memory and in tuning.json beside the kernel cache), which every later plan
+ * and batch of the class uses.  The candidates' kernels are compiled concurrently
+ * before the timing. */
 typedef struct {
     int32_t block, min_blocks_per_sm, variant;   /* the recorded shape */
     double samples_per_second;                   /* its rate */
