@@ -226,7 +226,7 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
     t_plans = time.perf_counter() - t0
     Ns = [x["N"] for x in inputs]
     tuned = None
-    if args.autotune:
+    if not args.no_autotune:
         # one representative per kernel class (topology, eps orders, regime): its mixed
         # launch shape and batch work item, recorded for every batch of the class
         t0 = time.perf_counter()
@@ -441,8 +441,8 @@ def main():
     ap.add_argument("--batch-only", action="store_true",
                     help="only the batched form (profiler captures); prints its object alone")
     ap.add_argument("--batch-fp64-scale", type=float, default=1 / 16)
-    ap.add_argument("--autotune", action="store_true",
-                    help="batched section: autotune each kernel class (ft_autotune) before the timed runs")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batched section: keep the default launch shapes instead of autotuning each kernel class")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -825,8 +825,12 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
             if (prec == 1) keys.push_back(pl->key(0, 0));
             ft::precompile_all(keys);
         }
+        // trials long enough for the steady state: at least 256 samples per thread of a
+        // full 512-thread-per-SM launch (shorter trials favour small blocks, which only
+        // balance the tail better)
+        const uint64_t tsamples = std::max<uint64_t>(samples, (uint64_t)dev_state().sms * 512ull * 256ull);
         ft_run_options o{};
-        o.num_samples = samples;
+        o.num_samples = tsamples;
         o.precision = precision;
         double best_rate = -1, default_rate = -1;
         ft::launch_shape best;
@@ -839,12 +843,12 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
             double rate = 0;
             try {
                 ft_run_options w = o;
-                w.num_samples = std::max<uint64_t>(1000, samples / 8);
-                run(*pl, w, pl->stream, nullptr);   // compiles and loads the candidate
+                w.num_samples = std::max<uint64_t>(1000, tsamples / 8);
+                run(*pl, w, pl->stream, nullptr);   // loads the candidate
                 for (int rep = 0; rep < 2; rep++) {
                     o.seed = (uint64_t)rep;
                     run_out ro = run(*pl, o, pl->stream, nullptr);
-                    rate = std::max(rate, (double)samples / (ro.kernel_ms * 1e-3));
+                    rate = std::max(rate, (double)tsamples / (ro.kernel_ms * 1e-3));
                 }
             } catch (...) {
                 pl->forced = false;
@@ -874,7 +878,7 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
         double best_batch = -1;
         unsigned long long best_chunk = 0;
         const uint64_t bsamples =
-            std::max<uint64_t>(samples, (uint64_t)dev_state().sms * (uint64_t)pl->key(prec, 0).block * 256ull * 4ull);
+            std::max<uint64_t>(tsamples, (uint64_t)dev_state().sms * (uint64_t)pl->key(prec, 0).block * 256ull * 4ull);
         for (unsigned long long c : {32ull, 64ull, 128ull, 256ull}) {
             ft::set_chunk_override(c);
             ft_batch* b = nullptr;

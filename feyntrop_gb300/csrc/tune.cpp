@@ -83,15 +83,16 @@ std::string tune_class(const kernel_key& k)
 launch_shape default_shape(const kernel_key& k)
 {
     // GB300 sweeps (double box, box-pentagon, K4, cube): the mixed form is bound by
-    // instruction fetch and gains 15-25 % from 512-thread blocks whose warps start each
-    // sample together (variant bit 2); deformed integrands also from out-of-line FP32
-    // transcendentals (bit 0).  The FP64 form is FP64-pipe bound (256 x 1); the
-    // per-sample barrier keeps its warps from drifting apart too (cube +10 %, double box
-    // +1 %).
+    // instruction fetch and gains 15-25 % from blocks whose warps start each sample
+    // together (variant bit 2); deformed integrands also from out-of-line FP32
+    // transcendentals (bit 0), and run best as two 256-thread blocks per SM (double box
+    // +0.8 %, box-pentagon batch +2 % over one 512-thread block, which undeformed ones
+    // keep).  The FP64 form is FP64-pipe bound (256 x 1); the per-sample barrier keeps
+    // its warps from drifting apart too (cube +10 %, double box +1 %).
     launch_shape s;
     if (k.prec == 1) {
-        s.block = 512;
-        s.minb = 1;
+        s.block = k.mode == 1 ? 256 : 512;
+        s.minb = k.mode == 1 ? 2 : 1;
     } else {
         s.block = 256;
         s.minb = 1;

@@ -202,7 +202,8 @@ int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds)
 /* Autotuner (no counterpart in the reference): times the sampling kernels of this plan's kernel class (topology, eps
  * orders, regime, precision) under candidate launch shapes (threads per block, blocks
  * per SM given to the register allocator, code-size variants), `samples` samples per
- * trial, then the batch work-item size (samples per thread: 32 .. 256) under the chosen
+ * trial (at least 256 per thread of a full launch, so that the trials see the steady
+ * state), then the batch work-item size (samples per thread: 32 .. 256) under the chosen
  * shape (batches of this integral with at least 1024 samples per thread of the GPU, so
  * that the largest item still leaves every SM several), and records both in the tuning
  * table (in memory and in tuning.json beside the kernel cache), which every later plan
