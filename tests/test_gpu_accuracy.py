@@ -1,0 +1,58 @@
+"""Per-sample accuracy of the mixed form at scale, against the plain-FP64 form on the
+same samples (the FP64 form itself is checked against the oracle in test_gpu_parity).
+The FP32 evaluation has a tail: on the benchmark's double box about one sample in
+250 000 ends above 1e-5 (the largest seen 1.4e-5), on random box-pentagon kinematics
+(deformation angles of tens of radians) a few in 100 000; both are bounded here."""
+import numpy as np
+import pytest
+
+import feyntrop_gb300 as ft
+from feyntrop_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def errors(plan, n, seed=0):
+    rm = plan.records(n, seed=seed, precision=ft.MIXED)
+    r6 = plan.records(n, seed=seed, precision=ft.FP64)
+    assert (rm["order"] == r6["order"]).all()
+    ok = (r6["flags"] & 1) == 0
+    assert ((rm["flags"][ok] & 1) == 0).all(), "mixed form dropped a sample the FP64 form kept"
+    scale = np.abs(r6["R"][ok]).max(axis=1)
+    e = np.abs(rm["R"][ok] - r6["R"][ok]).max(axis=1) / np.where(scale > 0, scale, 1.0)
+    return e, (rm["flags"] & 2) != 0
+
+
+def test_double_box_tail():
+    p = ft.Plan(workloads.double_box())
+    e, queued = errors(p, 1 << 18)
+    assert (e > 1e-5).sum() <= 3, np.sort(e)[-5:]
+    assert e.max() <= 2.5e-5, e.max()
+    assert np.quantile(e, 0.9999) <= 1e-5
+    assert np.median(e) < 1e-6
+    assert queued.mean() < 0.005
+    p.close()
+
+
+def test_random_box_pentagon_tail():
+    def accept(inp):
+        try:
+            ft.subgraph_table(inp)
+            return True
+        except ft.FeyntropError:
+            return False
+
+    inputs, _ = workloads.box_pentagon_scan(16, seed=11, accept=accept)
+    es, qs = [], []
+    for inp in inputs:
+        p = ft.Plan(inp)
+        e, q = errors(p, 8192, seed=2)
+        es.append(e)
+        qs.append(q)
+        p.close()
+    e = np.concatenate(es)
+    q = np.concatenate(qs)
+    assert np.quantile(e, 0.999) <= 1e-5, np.quantile(e, 0.999)
+    assert (e > 1e-5).mean() <= 5e-4, (e > 1e-5).mean()
+    assert e.max() <= 2.5e-5, e.max()
+    assert q.mean() < 0.03
