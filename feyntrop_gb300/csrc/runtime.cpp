@@ -870,16 +870,26 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
                 best = c;
             }
         }
+        // a candidate replaces the default only when clearly faster: trials of close
+        // shapes differ by run-to-run noise, and a one-integral trial does not rank close
+        // shapes reliably for the persistent batch kernel
+        const double kMargin = 1.03;
+        if (default_rate > 0 && best_rate < kMargin * default_rate) {
+            best = dflt;
+            best_rate = default_rate;
+        }
         best.rate = best_rate;
         ft::record_shape(pl->key(prec, 0), best);
         // the batch work item (samples per thread) of the class, under the chosen shape:
         // a batch of this one integral per candidate, with enough samples that even the
         // largest item leaves every SM four items
-        double best_batch = -1;
+        double best_batch = -1, default_batch = -1;
         unsigned long long best_chunk = 0;
+        const unsigned long long default_chunk = prec ? 128ull : 16ull;
         const uint64_t bsamples =
             std::max<uint64_t>(tsamples, (uint64_t)dev_state().sms * (uint64_t)pl->key(prec, 0).block * 256ull * 4ull);
-        for (unsigned long long c : {32ull, 64ull, 128ull, 256ull}) {
+        for (unsigned long long c : {16ull, 32ull, 64ull, 128ull, 256ull}) {
+            if (c == 16 && prec) continue;   // below the mixed default's range
             ft::set_chunk_override(c);
             ft_batch* b = nullptr;
             int rc = ft_batch_create(&pl, 1, prec, &b);
@@ -909,6 +919,11 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
                 best_batch = rate;
                 best_chunk = c;
             }
+            if (c == default_chunk) default_batch = rate;
+        }
+        if (default_batch > 0 && best_batch < kMargin * default_batch) {
+            best_batch = default_batch;
+            best_chunk = default_chunk;
         }
         best.chunk = best_chunk;
         ft::record_shape(pl->key(prec, 0), best);

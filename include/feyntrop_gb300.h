@@ -207,7 +207,8 @@ int ft_precompile(const ft_problem* problem, int32_t precision, double* seconds)
  * shape (batches of this integral with at least 1024 samples per thread of the GPU, so
  * that the largest item still leaves every SM several), and records both in the tuning
  * table (in memory and in tuning.json beside the kernel cache), which every later plan
- * and batch of the class uses.  The candidates' kernels are compiled concurrently
+ * and batch of the class uses.  A candidate replaces the default shape or work item
+ * only when it is at least 3 % faster in these trials.  The candidates' kernels are compiled concurrently
  * before the timing. */
 typedef struct {
     int32_t block, min_blocks_per_sm, variant;   /* the recorded shape */
