@@ -325,7 +325,7 @@ void record(ft_batch& b)
             qacc = b.d_qacc + g.off_qacc;
             const unsigned long long* cq = g.d_queue;
             const unsigned int* cqc = qcount;
-            void* qargs[] = {&inst, &ninst, &item_state, &lanepw, &lanebits, &cq, &cqc, &qcap, &qacc};
+            void* qargs[] = {&inst, &ninst, &cq, &cqc, &qcap, &qacc};
             ft::check(ft::drv().LaunchKernel(g.k64->queue, g.qgrid, 1, 1, g.k64->block, 1, 1, 0,
                                              (CUstream)g.stream, qargs, nullptr),
                       "launch ft_sample_queue_batch");
@@ -387,7 +387,7 @@ bool ensure_capacity(ft_batch& b, const std::vector<size_t>& qwant)
             cudaFree(g.d_queue);
             g.d_queue = nullptr;
             g.qcap = 0;
-            cu(cudaMalloc(&g.d_queue, cap * 8), "cudaMalloc(batch FP64 queue)");
+            cu(cudaMalloc(&g.d_queue, cap * 5 * 8), "cudaMalloc(batch FP64 queue)");
             g.qcap = cap;
             grew = true;
         }
@@ -452,7 +452,7 @@ int ft_batch_run(ft_batch* b, const ft_run_options* opts, ft_result* results)
                 p->first_item = next;
                 p->nitems = items;
                 next += items;
-                q += (size_t)std::min<unsigned long long>(N, N / 32 + 1024);
+                q += (size_t)std::min<unsigned long long>(N, N / 64 + 1024);
             }
             if (next >= (1ull << 36)) throw std::invalid_argument("ft_batch_run: too many work items");
             g.total_items = next;

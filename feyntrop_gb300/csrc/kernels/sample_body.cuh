@@ -2055,9 +2055,9 @@ static __device__ __forceinline__ void sample64(xo& g, const table_ref& tr, cons
 // ------------------------------------------------------------------ one thread's samples
 // Samples [first, last) of the stream, g holding the state of sample `first`.  In the
 // mixed form, samples whose FP32 evaluation is not trustworthy are queued for the FP64
-// pass and left out of the sums here: 5 words (sample index, stream state) in the
-// single-integral kernels, one word `qtag | (i - first)` in the batch kernels (the
-// FP64 pass re-derives the state from the work item).
+// pass and left out of the sums here: 5 words, the sample (its index in the
+// single-integral kernels, `qtag | (i - first)` naming the work item in the batch
+// kernels) and its stream state.
 static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, const double* __restrict__ prm,
                                                     u64 first, u64 last, u64 chunk, accum& A, u64* __restrict__ queue,
                                                     unsigned int* __restrict__ qcount, unsigned int qcap, u64 qtag,
@@ -2102,16 +2102,16 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
             A.note32(0.0f, 1.0f, (float)ex);
             const unsigned int slot = atomicAdd(qcount, 1u);
             if (slot < qcap) {
-#if FT_BATCH
-                queue[slot] = qtag | (i - first);
-#else
                 u64* q = queue + (size_t)slot * 5;
+#if FT_BATCH
+                q[0] = qtag | (i - first);
+#else
                 q[0] = i;
+#endif
                 q[1] = g0.a;
                 q[2] = g0.b;
                 q[3] = g0.c;
                 q[4] = g0.d;
-#endif
             }
             if (FT_RECORD) write_record(i, ord, R, false, flags, rec_order, rec_R, rec_flags);
             continue;
@@ -2210,7 +2210,8 @@ struct batch_inst {
     u64 pad[3];
 };
 
-// FP64-pass queue word: item << 28 | lane << 18 | offset of the sample in the lane's chunk
+// first word of an FP64-pass queue entry: item << 28 | lane << 18 | offset of the
+// sample in the lane's chunk (the other four hold the sample's stream state)
 #define BQ_ITEM_SHIFT 28
 #define BQ_LANE_SHIFT 18
 #define BQ_OFF_MASK ((1ull << BQ_LANE_SHIFT) - 1ull)
@@ -2273,34 +2274,25 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample_batch(
 }
 
 #if FT_PREC == 0
-// FP64 pass over the samples a mixed batch launch queued.  Each entry names its work
-// item, lane and offset; the stream state is re-derived (item state, the mixed
-// launch's lane skip, offset * (2E-1) steps).  Sums go to the instance's slots of
-// qacc with atomics: per eps order j [4j + 0..3] = re f, re f^2, im f, im f^2, then
-// [4K] kept, [4K+1] dropped, [4K+2] robust.
+// FP64 pass over the samples a mixed batch launch queued: each entry names its work
+// item (hence the instance) and carries the sample's stream state.  Sums go to the
+// instance's slots of qacc with atomics: per eps order j [4j + 0..3] = re f, re f^2,
+// im f, im f^2, then [4K] kept, [4K+1] dropped, [4K+2] robust.
 #define QACC_SLOTS (4 * FT_K + 4)
 extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue_batch(
-    const batch_inst* __restrict__ inst, int ninst, const u64* __restrict__ item_state,
-    const u64* __restrict__ lanepw, int lanebits, const u64* __restrict__ queue,
+    const batch_inst* __restrict__ inst, int ninst, const u64* __restrict__ queue,
     const unsigned int* __restrict__ qcount, unsigned int qcap, double* __restrict__ qacc)
 {
     unsigned int n = *qcount;
     if (n > qcap) n = qcap;
-    const unsigned int lane = threadIdx.x & 31u;
-    const unsigned int warp0 = (blockIdx.x * blockDim.x + threadIdx.x) - lane;
-    const unsigned int stride = gridDim.x * blockDim.x;
-    // warp-uniform trip count: skip_lanes needs the whole warp
-    for (unsigned int k0 = warp0; k0 < n; k0 += stride) {
-        const unsigned int k = k0 + lane;
-        const bool active = k < n;
-        const u64 w = active ? queue[k] : 0ull;
-        const u64 item = w >> BQ_ITEM_SHIFT;
-        const u32 ln = active ? (u32)((w >> BQ_LANE_SHIFT) & BQ_LANE_MASK) : 0u;
-        const u64 off = w & BQ_OFF_MASK;
-        xo g = load_state(item_state + item * 4);
-        skip_lanes(g, ln, lanepw, lanebits);
-        if (!active) continue;
-        for (u64 s = 0; s < off * (2 * FT_E - 1); s++) g.next();
+    for (unsigned int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const u64* q = queue + (size_t)k * 5;
+        const u64 item = q[0] >> BQ_ITEM_SHIFT;
+        xo g;
+        g.a = q[1];
+        g.b = q[2];
+        g.c = q[3];
+        g.d = q[4];
         const int id = find_instance(inst, ninst, item);
         const double* prm = inst[id].prm;
         const unsigned char* tab = inst[id].tab;
@@ -2319,21 +2311,21 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue_batch(
         draw_sector64(g, tr, prm[P_JRFULL], X, F, Gv, ord);
         bool rob = false;
         const bool ok = integrand64(prm, X, F, Gv * F, R, rob);
-        double* q = qacc + (size_t)id * QACC_SLOTS;
-        if (rob) atomicAdd(q + 4 * FT_K + 2, 1.0);
+        double* qa = qacc + (size_t)id * QACC_SLOTS;
+        if (rob) atomicAdd(qa + 4 * FT_K + 2, 1.0);
         if (!ok) {
-            atomicAdd(q + 4 * FT_K + 1, 1.0);
+            atomicAdd(qa + 4 * FT_K + 1, 1.0);
             continue;
         }
-        atomicAdd(q + 4 * FT_K, 1.0);
+        atomicAdd(qa + 4 * FT_K, 1.0);
 #pragma unroll
         for (int j = 0; j < FT_K; j++) {
             if (FT_ONLY_PSI && j > 0) break;
-            atomicAdd(q + 4 * j + 0, R[j].re);
-            atomicAdd(q + 4 * j + 1, R[j].re * R[j].re);
+            atomicAdd(qa + 4 * j + 0, R[j].re);
+            atomicAdd(qa + 4 * j + 1, R[j].re * R[j].re);
             if (ACC_PARTS == 4) {
-                atomicAdd(q + 4 * j + 2, R[j].im);
-                atomicAdd(q + 4 * j + 3, R[j].im * R[j].im);
+                atomicAdd(qa + 4 * j + 2, R[j].im);
+                atomicAdd(qa + 4 * j + 3, R[j].im * R[j].im);
             }
         }
     }
