@@ -32,7 +32,10 @@ unsigned table_smem_bytes(const kernel_key& k)
     const unsigned tab = k.table_global ? 0u : (k.prec == 0 ? 25u * entries : 17u * entries);
     const unsigned parts = k.mode == 1 ? 4u : 2u;
     const unsigned acc = (unsigned)k.block * parts * (unsigned)k.K * (k.prec == 0 ? 16u : 24u);
-    return ((tab + 15u) & ~15u) + acc;
+    // the V pass buffer (mixed deformed kernels with variant bits 2 and 3)
+    const unsigned vbuf =
+        (k.prec == 1 && k.mode == 1 && (k.variant & 12) == 12) ? 16u + 2u * (unsigned)k.block * 40u : 0u;
+    return ((tab + 15u) & ~15u) + acc + vbuf;
 }
 
 // Tables of the two-float logarithm and exponential of the mixed kernels (FP32 values

@@ -65,7 +65,8 @@ typedef unsigned int u32;
 // transcendental, bit 1 does the same for the two-float primitives, so the code the
 // SM streams per sample fits the instruction caches better; bit 2 starts every sample
 // with a block-wide barrier, so that the block's warps walk the code together and
-// share its instruction fetches.
+// share its instruction fetches; bit 3 (with bit 2, deformed mixed kernels) adds the
+// V pass below.
 #ifndef FT_VARIANT
 #define FT_VARIANT 0
 #endif
@@ -137,6 +138,16 @@ static __device__ FT_MATHFN void m_sincos(float x, float* s, float* c) { sincosf
 #define REC_QUEUED 2
 #define REC_EXACT 4
 #define REC_ROBUST 8
+#define REC_VPASS 16
+// V pass (FT_VARIANT bit 3, with the per-sample barrier, deformed mixed kernels):
+// samples rejected only for the FP32 rounding of V are collected per block in shared
+// memory and re-evaluated, all threads of the block together, with V in two-float
+#if FT_PREC == 1 && FT_MODE == 1 && (FT_VARIANT & 12) == 12
+#define FT_VPASS 1
+#else
+#define FT_VPASS 0
+#endif
+#define ACC_VPASS (8 * FT_K + 5)
 
 // ------------------------------------------------------------------ small helpers
 static __device__ __forceinline__ u64 rotl64(u64 x, int k) { return (x << k) | (x >> (64 - k)); }
@@ -1172,6 +1183,163 @@ static __device__ __forceinline__ df df_of(f2 x)
     return r;
 }
 
+#if FT_VPASS
+// ------------------------------------------------------------------ V in two-float (V pass)
+// Complex two-float numbers, and sin / cos of a two-float angle to ~1e-14: the angle is
+// reduced by the nearest multiple k of pi/2 (pi/2 as a three-part constant, each k * part
+// formed exactly with an FMA), then sin and cos of the reduced r in [-pi/4, pi/4] come
+// from their Taylor series, r (1 - z/3! + z^2/5! - ...) and 1 - z/2! + z^2/4! - ...
+// with z = r^2, summed by Horner's rule in two-float (coefficients 1/n! as float pairs;
+// the series is cut where z^k/n! < 1e-16).
+struct cdf {
+    df re, im;
+};
+static __device__ __forceinline__ cdf cdf_mk(df r, df i)
+{
+    cdf z;
+    z.re = r;
+    z.im = i;
+    return z;
+}
+static __device__ __forceinline__ cdf cdf_zero() { return cdf_mk(df_mk(0.0f), df_mk(0.0f)); }
+static __device__ __forceinline__ cdf operator+(cdf a, cdf b) { return cdf_mk(df_add(a.re, b.re), df_add(a.im, b.im)); }
+static __device__ __forceinline__ cdf operator-(cdf a, cdf b) { return cdf_mk(df_sub(a.re, b.re), df_sub(a.im, b.im)); }
+static __device__ __forceinline__ cdf operator*(cdf a, cdf b)
+{
+    return cdf_mk(df_fma(a.re, b.re, df_neg(df_mul(a.im, b.im))), df_fma(a.re, b.im, df_mul(a.im, b.re)));
+}
+static __device__ __forceinline__ cdf operator*(df s, cdf a) { return cdf_mk(df_mul(s, a.re), df_mul(s, a.im)); }
+static __device__ __forceinline__ cdf cdf_inv(cdf a)
+{
+    const df m = df_inv(df_fma(a.re, a.re, df_mul(a.im, a.im)));
+    return cdf_mk(df_mul(a.re, m), df_neg(df_mul(a.im, m)));
+}
+
+static __device__ __forceinline__ void sincos_df(df x, df& s, df& c)
+{
+    const float P1 = 0x1.921fb6p+0f, P2 = -0x1.777a5cp-25f, P3 = -0x1.ee59dap-50f;
+    const float k = rintf((x.hi + x.lo) * 0x1.45f306p-1f);
+    const float p1 = k * P1, e1 = fmaf(k, P1, -p1);
+    const float p2 = k * P2, e2 = fmaf(k, P2, -p2);
+    df r = df_add(x, df_norm(-p1, -e1));
+    r = df_add(r, df_norm(-p2, -e2));
+    r = df_add(r, df_mk(-k * P3));
+    const df z = df_mul(r, r);
+    // (-1)^j / (2j+1)!, j = 0..7, and (-1)^j / (2j)!, j = 0..8, as (hi, lo)
+    const float SN[8][2] = {{1.0f, 0.0f},
+                            {-0x1.555556p-3f, 0x1.555556p-28f},
+                            {0x1.111112p-7f, -0x1.dddddep-32f},
+                            {-0x1.a01a02p-13f, 0x1.7f97fap-39f},
+                            {0x1.71de3ap-19f, 0x1.55b1ccp-45f},
+                            {-0x1.ae6456p-26f, -0x1.fd5138p-52f},
+                            {0x1.612462p-33f, -0x1.8af25ep-58f},
+                            {-0x1.ae7f3ep-41f, -0x1.ccee08p-67f}};
+    const float CS[9][2] = {{1.0f, 0.0f},
+                            {-0.5f, 0.0f},
+                            {0x1.555556p-5f, -0x1.555556p-30f},
+                            {-0x1.6c16c2p-10f, 0x1.27d27ep-35f},
+                            {0x1.a01a02p-16f, -0x1.7f97fap-42f},
+                            {-0x1.27e4fcp-22f, 0x1.10ec14p-47f},
+                            {0x1.1eed8ep-29f, 0x1.ff1b14p-54f},
+                            {-0x1.93974ap-37f, -0x1.180f94p-62f},
+                            {0x1.ae7f3ep-45f, 0x1.ccee08p-71f}};
+    df ps, pc;
+    ps.hi = SN[7][0];
+    ps.lo = SN[7][1];
+#pragma unroll
+    for (int j = 6; j >= 0; j--) {
+        df cj;
+        cj.hi = SN[j][0];
+        cj.lo = SN[j][1];
+        ps = df_fma(ps, z, cj);
+    }
+    pc.hi = CS[8][0];
+    pc.lo = CS[8][1];
+#pragma unroll
+    for (int j = 7; j >= 0; j--) {
+        df cj;
+        cj.hi = CS[j][0];
+        cj.lo = CS[j][1];
+        pc = df_fma(pc, z, cj);
+    }
+    const df sr = df_mul(r, ps);
+    const int q = ((int)k) & 3;
+    s = (q == 0) ? sr : (q == 1) ? pc : (q == 2) ? df_neg(sr) : df_neg(pc);
+    c = (q == 0) ? pc : (q == 1) ? df_neg(sr) : (q == 2) ? df_neg(pc) : sr;
+}
+
+// V = -sum_r sigma_r q_r^T L(y)^-1 q_r + sum_e m2_e X_e e^(i theta_e) at the deformed point,
+// in two-float complex arithmetic: conductances y_e = e^(-i theta_e) / X_e from the
+// two-float contour and sector point, the same conductance-form elimination as `elim`,
+// the quadratic forms with sigma and q as two-float pairs.
+static __device__ __forceinline__ cdf v_twofloat(const df* theta, const f2* Xi2, const float* pd)
+{
+    auto pdf = [&](int i) -> df {
+        df v;
+        v.hi = pd[2 * i];
+        v.lo = pd[2 * i + 1];
+        return v;
+    };
+    cdf y[FT_E];
+    cdf v = cdf_zero();
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        df sn, cs;
+        sincos_df(theta[e], sn, cs);
+        const df xi = df_of(Xi2[e]);
+        y[e] = cdf_mk(df_mul(xi, cs), df_neg(df_mul(xi, sn)));
+        const df x = df_inv(xi);
+        v = v + pdf(P_M2 + e) * cdf_mk(df_mul(x, cs), df_mul(x, sn));
+    }
+    cdf c[FT_N][FT_N], g[FT_N];
+#pragma unroll
+    for (int i = 0; i < FT_N; i++) {
+        g[i] = cdf_zero();
+#pragma unroll
+        for (int j = 0; j < FT_N; j++) c[i][j] = cdf_zero();
+    }
+#pragma unroll
+    for (int e = 0; e < FT_E; e++) {
+        const int k = FT_EK[e], l = FT_EL[e];
+        if (k == FT_V - 1)
+            g[l] = g[l] + y[e];
+        else
+            c[l][k] = c[l][k] + y[e];
+    }
+    cdf a[FT_N][FT_N], dinv[FT_N];
+#pragma unroll
+    for (int k = 0; k < FT_N; k++) {
+        cdf dk = g[k];
+#pragma unroll
+        for (int j = k + 1; j < FT_N; j++) dk = dk + c[k][j];
+        dinv[k] = cdf_inv(dk);
+#pragma unroll
+        for (int i = k + 1; i < FT_N; i++) a[k][i] = c[k][i] * dinv[k];
+#pragma unroll
+        for (int i = k + 1; i < FT_N; i++) {
+            g[i] = g[i] + a[k][i] * g[k];
+#pragma unroll
+            for (int j = i + 1; j < FT_N; j++) c[i][j] = c[i][j] + a[k][i] * c[k][j];
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < FT_RANK; r++) {
+        cdf yv[FT_N];
+        cdf sr = cdf_zero();
+#pragma unroll
+        for (int i = 0; i < FT_N; i++) {
+            cdf yi = cdf_mk(pdf(P_Q + r * FT_N + i), df_mk(0.0f));
+#pragma unroll
+            for (int k = 0; k < i; k++) yi = yi + a[k][i] * yv[k];
+            yv[i] = yi;
+            sr = sr + (yi * yi) * dinv[i];
+        }
+        v = v - pdf(P_SIG + r) * sr;
+    }
+    return v;
+}
+#endif
+
 // x-derivatives of phi/psi at the sample point (srcs/laplacian.hpp:102-215) and the
 // deformation angle theta = -lambda (d(phi/psi)/dx + m^2) (srcs/feynman_integral.hpp:290-291).
 // Everything here is a difference of entries of L^-1, which cancels in FP32 for a
@@ -1410,10 +1578,13 @@ static __device__ __forceinline__ f2 wrap_pi2(f2 x, bool& edge)
     return r;
 }
 
+// VX: V in two-float (the V pass); vfail reports a hand-off for V's rounding alone
+template <bool VX>
 static __device__ __forceinline__ bool integrand32(const float* pd, const float* pf, const f2* lx, f2 lF, f2 lG,
-                                                   cx<float>* out, bool& need64)
+                                                   cx<float>* out, bool& need64, bool& vfail)
 {
     need64 = false;
+    vfail = false;
     const float D2 = 0.5f * pf[P_D], W = pf[P_W];
     // working frame X_e = exp(lx_e - sh), sh an integer near the middle of the range;
     // R and the eps factor are ratios to the tropical approximants and do not depend on it
@@ -1571,21 +1742,30 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     cx<float> cpphi = cmk(0.0f, 0.0f);
     float mag = 0.0f;
     float qmag = 0.0f;   // magnitude of the terms summed into V, through the eliminations
+    cx<float> cV;
+#if FT_VPASS
+    if constexpr (VX) {
+        const cdf vd = v_twofloat(theta, Xi2, pd);
+        cV = cmk(vd.re.hi + vd.re.lo, vd.im.hi + vd.im.lo);
+    } else
+#endif
+    {
 #pragma unroll
-    for (int r = 0; r < FT_RANK; r++) {
-        float qm = 0.0f;
-        const cx<float> v = pf[P_SIG + r] * CL.quad_mag(pf + P_Q + r * FT_N, qm);
-        qmag += fabsf(pf[P_SIG + r]) * qm;
-        cpphi = cpphi - v;
-        mag += cabs_(v);
-    }
-    cx<float> cV = cpphi;
+        for (int r = 0; r < FT_RANK; r++) {
+            float qm = 0.0f;
+            const cx<float> v = pf[P_SIG + r] * CL.quad_mag(pf + P_Q + r * FT_N, qm);
+            qmag += fabsf(pf[P_SIG + r]) * qm;
+            cpphi = cpphi - v;
+            mag += cabs_(v);
+        }
+        cV = cpphi;
 #pragma unroll
-    for (int e = 0; e < FT_E; e++) {
-        cV = cV + pf[P_M2 + e] * cX[e];
-        mag += pf[P_M2 + e] * X[e];
+        for (int e = 0; e < FT_E; e++) {
+            cV = cV + pf[P_M2 + e] * cX[e];
+            mag += pf[P_M2 + e] * X[e];
+        }
+        qmag += mag;
     }
-    qmag += mag;
     const float vabs = cabs_(cV);
     FT_DBG(20, cV.re);
     FT_DBG(21, cV.im);
@@ -1596,8 +1776,9 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     // is bounded by the magnitudes of the terms they sum (qmag: sum_r |sigma_r|
     // sum_i |y_i^2 / d_i| of the forward substitutions, plus the mass terms); V^-W
     // turns it into a relative error of about 1e-7 W qmag / |V|.
-    if (!(vabs > V_CANCEL * mag) || !(W * qmag < V_AMPLIFY * vabs)) {
+    if (!VX && (!(vabs > V_CANCEL * mag) || !(W * qmag < V_AMPLIFY * vabs))) {
         need64 = true;
+        vfail = true;
         return false;
     }
 
@@ -1887,7 +2068,7 @@ struct accum {
     int since_fold;
     float keptf, droppedf, queuedf, exactf;   // counters below 2^24 between folds
 #endif
-    double kept, dropped, queued, exact, robust;
+    double kept, dropped, queued, exact, robust, vpass;
 
     __device__ __forceinline__ void init(unsigned char* smem_acc)
     {
@@ -1909,7 +2090,7 @@ struct accum {
             Cf[s * FT_BLOCK] = 0.0f;
 #endif
         }
-        kept = dropped = queued = exact = robust = 0.0;
+        kept = dropped = queued = exact = robust = vpass = 0.0;
     }
 
     __device__ __forceinline__ void nadd(int slot, double v)
@@ -2004,6 +2185,7 @@ struct accum {
         vals[ACC_ROBUST] = robust;
 #pragma unroll
         for (int s = ACC_ROBUST + 1; s < ACC_SLOTS; s++) vals[s] = 0.0;
+        vals[ACC_VPASS] = vpass;
         block_reduce(vals, dst);
     }
 };
@@ -2052,6 +2234,30 @@ static __device__ __forceinline__ void sample64(xo& g, const table_ref& tr, cons
 }
 #endif
 
+#if FT_VPASS
+// the V pass buffer after the per-thread sums: 2 FT_BLOCK entries of 5 words (the
+// sample as in the FP64 queue, and its stream state), then the entry count
+#define VBUF_OFFSET ((ACC_SMEM_OFFSET + FT_BLOCK * ACC_BYTES_PER_THREAD + 15u) & ~15u)
+// one sample of the V pass from its stream state: the sector redrawn, the integrand
+// with V in two-float; 0 kept, 1 dropped, 2 for the FP64 pass
+static __device__ __noinline__ int vpass_eval(u64 sa, u64 sb, u64 sc, u64 sd, const table_ref* tr, const float* pf,
+                                             const float* pd, cx<float>* R, unsigned char* ord)
+{
+    xo g;
+    g.a = sa;
+    g.b = sb;
+    g.c = sc;
+    g.d = sd;
+    f2 lx[FT_E], lF, lG;
+    draw_sector32(g, *tr, pf, lx, lF, lG, ord);
+#pragma unroll
+    for (int j = 0; j < FT_K; j++) R[j] = cmk(0.0f, 0.0f);
+    bool need64 = false, vfail = false;
+    const bool ok = integrand32<true>(pd, pf, lx, lF, lG, R, need64, vfail);
+    return need64 ? 2 : (ok ? 0 : 1);
+}
+#endif
+
 // ------------------------------------------------------------------ one thread's samples
 // Samples [first, last) of the stream, g holding the state of sample `first`.  In the
 // mixed form, samples whose FP32 evaluation is not trustworthy are queued for the FP64
@@ -2070,12 +2276,58 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
 #endif
     (void)qtag;
     (void)chunk;
+#if FT_VPASS
+    extern __shared__ __align__(16) unsigned char smem[];
+    u64* vbuf = (u64*)(smem + VBUF_OFFSET);
+    unsigned int* vcnt = (unsigned int*)(vbuf + 2 * FT_BLOCK * 5);
+    if (threadIdx.x == 0) *vcnt = 0u;
+    // entries [n - m, n) of the buffer, one per thread
+    auto vflush = [&](unsigned int n, unsigned int m) {
+        if (threadIdx.x < m) {
+            const u64* v = vbuf + (size_t)(n - m + threadIdx.x) * 5;
+            cx<float> Rv[FT_K];
+            unsigned char ordv[FT_E];
+            const int st = vpass_eval(v[1], v[2], v[3], v[4], &tr, pf, pd, Rv, ordv);
+            unsigned char fl = REC_VPASS;
+            A.vpass += 1.0;
+            if (st == 2) {
+                fl |= REC_QUEUED;
+                A.note32(0.0f, 1.0f, 0.0f);
+                const unsigned int slot = atomicAdd(qcount, 1u);
+                if (slot < qcap) {
+                    u64* q = queue + (size_t)slot * 5;
+#pragma unroll
+                    for (int w = 0; w < 5; w++) q[w] = v[w];
+                }
+            } else if (st == 1) {
+                fl |= REC_DROPPED;
+                A.note32(1.0f, 0.0f, 0.0f);
+            } else {
+                A.add32(Rv);
+            }
+#if !FT_BATCH
+            if (FT_RECORD) write_record(v[0], ordv, Rv, st == 0, fl, rec_order, rec_R, rec_flags);
+#endif
+        }
+    };
+#endif
 #if FT_VARIANT & 4
     // Every thread of the block makes `chunk` trips and the block starts each sample
     // together: the warps then run the same stretch of the (long, straight-line)
     // per-sample code at the same time and share its instruction fetches.
     for (u64 k = 0; k < chunk; k++) {
         __syncthreads();
+#if FT_VPASS
+        {
+            const unsigned int n = *vcnt;   // the same for the whole block (read after the barrier)
+            if (n >= FT_BLOCK) {
+                vflush(n, FT_BLOCK);
+                __syncthreads();
+                if (threadIdx.x == 0) *vcnt = n - FT_BLOCK;
+                __syncthreads();
+            }
+        }
+#endif
         const u64 i = first + k;
         if (i >= last) continue;
 #else
@@ -2095,8 +2347,29 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
         if (ex) flags |= REC_EXACT;
         if (FT_RECORD)
             for (int e = 0; e < FT_E; e++) rec_X[i * FT_E + e] = exp((double)lx[e].hi + (double)lx[e].lo);
-        bool need64 = false;
-        const bool ok = integrand32(pd, pf, lx, lF, lG, R, need64);
+        bool need64 = false, vfail = false;
+        const bool ok = integrand32<false>(pd, pf, lx, lF, lG, R, need64, vfail);
+        (void)vfail;
+#if FT_VPASS
+        if (need64 && vfail) {
+            // fewer than FT_BLOCK entries before this sample: the slot stays in the buffer
+            const unsigned int s2 = atomicAdd(vcnt, 1u);
+            u64* v = vbuf + (size_t)s2 * 5;
+#if FT_BATCH
+            v[0] = qtag | (i - first);
+#else
+            v[0] = i;
+#endif
+            v[1] = g0.a;
+            v[2] = g0.b;
+            v[3] = g0.c;
+            v[4] = g0.d;
+            A.note32(0.0f, 0.0f, (float)ex);
+            if (FT_RECORD)
+                write_record(i, ord, R, false, (unsigned char)(flags | REC_VPASS), rec_order, rec_R, rec_flags);
+            continue;
+        }
+#endif
         if (need64) {
             flags |= REC_QUEUED;
             A.note32(0.0f, 1.0f, (float)ex);
@@ -2126,6 +2399,19 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
         if (FT_RECORD) write_record(i, ord, R, ok, flags, rec_order, rec_R, rec_flags);
 #endif
     }
+#if FT_VPASS
+    // the rest of the buffer, in rounds of at most FT_BLOCK entries
+    __syncthreads();
+    {
+        unsigned int n = *vcnt;
+        while (n > 0) {
+            const unsigned int m = n < FT_BLOCK ? n : FT_BLOCK;
+            vflush(n, m);
+            n -= m;
+        }
+    }
+    __syncthreads();
+#endif
 }
 
 #if !FT_BATCH

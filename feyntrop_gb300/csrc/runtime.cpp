@@ -808,7 +808,12 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
             const int v = deformed ? 1 : 0;
             for (int var : {v | 4, v})
                 for (int bm : {512, 256, 128}) add(bm, 512 / bm, var);
-            if (deformed) add(512, 1, 4);
+            if (deformed) {
+                add(512, 1, 4);
+                // the V pass (bit 3): pays where many samples fail only for V's rounding
+                add(256, 2, 13);
+                add(512, 1, 13);
+            }
         } else {
             const int v = deformed ? 1 : 0;
             for (int var : {v | 4, v})

@@ -87,8 +87,9 @@ launch_shape default_shape(const kernel_key& k)
     // together (variant bit 2); deformed integrands also from out-of-line FP32
     // transcendentals (bit 0), and run best as two 256-thread blocks per SM (double box
     // +0.8 %, box-pentagon batch +2 % over one 512-thread block, which undeformed ones
-    // keep).  The FP64 form is FP64-pipe bound (256 x 1); the per-sample barrier keeps
-    // its warps from drifting apart too (cube +10 %, double box +1 %).
+    // keep).  Bit 3 (the V pass) is left to the autotuner.  The FP64 form is FP64-pipe
+    // bound (256 x 1); the per-sample barrier keeps its warps from drifting apart too
+    // (cube +10 %, double box +1 %).
     launch_shape s;
     if (k.prec == 1) {
         s.block = k.mode == 1 ? 256 : 512;

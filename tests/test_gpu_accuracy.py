@@ -56,3 +56,42 @@ def test_random_box_pentagon_tail():
     assert (e > 1e-5).mean() <= 5e-4, (e > 1e-5).mean()
     assert e.max() <= 2.5e-5, e.max()
     assert q.mean() < 0.03
+
+
+def test_v_pass_variant_keeps_the_accuracy_with_fewer_fp64_hand_offs():
+    """Code variant bit 3 (an autotuner candidate for deformed classes): samples rejected
+    only for V's FP32 rounding are re-evaluated with V in two-float instead of going to
+    the FP64 pass.  Same accuracy tail, fewer FP64 hand-offs, the same integral."""
+    import os
+
+    def accept(inp):
+        try:
+            ft.subgraph_table(inp)
+            return True
+        except ft.FeyntropError:
+            return False
+
+    inp = workloads.box_pentagon_scan(4, seed=11, accept=accept)[0][1]
+    os.environ["FEYNTROP_GB300_VARIANT"] = "13"
+    try:
+        p = ft.Plan(inp)
+        e13, _ = errors(p, 1 << 15, seed=4)
+        rec = p.records(1 << 15, seed=4, precision=ft.MIXED)
+        r13 = p.integrate(2_000_000, seed=6, precision=ft.MIXED)
+        p.close()
+    finally:
+        del os.environ["FEYNTROP_GB300_VARIANT"]
+    p = ft.Plan(inp)
+    e5, _ = errors(p, 1 << 15, seed=4)
+    r5 = p.integrate(2_000_000, seed=6, precision=ft.MIXED)
+    p.close()
+    assert ((rec["flags"] & 16) != 0).any(), "no sample took the V pass"
+    assert np.quantile(e13, 0.999) <= max(1e-5, 1.5 * np.quantile(e5, 0.999))
+    assert e13.max() <= 2.5e-5
+    assert r13["fp64_fallback"] < r5["fp64_fallback"]
+    assert r13["kept"] + r13["dropped"] == 2_000_000
+    for j in range(len(r5["integral"])):
+        for part in range(2):
+            x, dx = r5["integral"][j][part]
+            y = r13["integral"][j][part][0]
+            assert abs(x - y) <= 0.02 * dx + 1e-300, (j, part, x, y, dx)
