@@ -28,7 +28,10 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("FEYNTROP_REFERENCE", "/root/reference")
+REF = os.environ.get("FEYNTROP_REFERENCE")
+if not REF or not os.path.isdir(os.path.join(REF, "srcs")):
+    sys.exit("make_golden.py: set FEYNTROP_REFERENCE to a checkout of the reference (its srcs/ and "
+             "py_feyntrop.py), and build oracle/_ref with `make -C oracle ref REF=$FEYNTROP_REFERENCE`")
 REF_BIN = os.path.join(REPO, "oracle", "_ref", "feyntrop")
 HARNESS = os.path.join(REPO, "oracle", "_ref", "ref_harness")
 
