@@ -16,10 +16,12 @@ reported time is the max over ranks.  `e2e` repeats the step through the public
 API as a user calls it (plan creation with host preprocessing and the upload of
 the table, integration, result read-back) timed on the host.
 
-Batched form (`batched` in the line, --batched scan|mixed|none): a whole seeded batch
-of integrals (4096 box-pentagon kinematic points by default) per run, one CUDA graph
-launch with one persistent sampling launch per topology class, mixed precision
-against plain FP64 on the same integrals.
+Batched form (`batched` in the line, --batched both|scan|mixed|none): a whole seeded
+batch of integrals per run, one CUDA graph launch with one persistent sampling launch
+per topology class, mixed precision against plain FP64 on the same integrals.  By
+default both workloads: the 4096-point box-pentagon kinematic scan and the mixed
+uneven batch (1536 integrals of four topologies), each with the per-sample error of
+every kernel class.
 
 Multi-GPU (torchrun): rank r integrates its own block of N samples of the same
 stream (samples [rN, (r+1)N)); the merged moments equal a single run over all
@@ -162,9 +164,10 @@ def dist_env():
     return rank, world, local
 
 
-def cpu_rate(inp, seconds, threads, kind_pref=("reference", "port")):
-    """Samples/s of the reference's CPU loop on this host: the reference binary when it
-    is built and runs here, else the restatement built with the reference's flags."""
+def cpu_rate(inp, seconds, threads, kind_pref=("reference", "port"), n=None):
+    """(samples/s, samples, kind) of the reference's CPU loop on this host: the reference
+    binary when it is built and runs here, else the restatement built with the
+    reference's flags.  n samples, or (n=None) as many as take about `seconds`."""
     ref_bin = os.path.join(HERE, "oracle", "_ref", "feyntrop")
     env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     if "reference" in kind_pref and os.path.exists(ref_bin):
@@ -173,7 +176,8 @@ def cpu_rate(inp, seconds, threads, kind_pref=("reference", "port")):
                                    env=env, timeout=120)
             if probe.returncode == 0:
                 r0 = 20000 / max(json.loads(probe.stdout)["seconds sampling"], 1e-6)
-                n = int(max(1e5, min(r0 * seconds, 5e8)))
+                if n is None:
+                    n = int(max(1e5, min(r0 * seconds, 5e8)))
                 out = subprocess.run([ref_bin], input=json.dumps(dict(inp, N=n)), capture_output=True, text=True,
                                      env=env, timeout=600)
                 t = json.loads(out.stdout)["seconds sampling"]
@@ -183,16 +187,17 @@ def cpu_rate(inp, seconds, threads, kind_pref=("reference", "port")):
     sys.path.insert(0, os.path.join(HERE, "tests"))
     import oracle_lib  # the oracle's CPU restatement: the baseline only, never the measured GPU path
     p = oracle_lib.Prepared(inp, fast=True)
-    t0 = time.perf_counter()
-    p.integrate(50000, 0, threads)
-    r0 = 50000 / (time.perf_counter() - t0)
-    n = int(max(1e5, min(r0 * seconds, 5e8)))
+    if n is None:
+        t0 = time.perf_counter()
+        p.integrate(50000, 0, threads)
+        r0 = 50000 / (time.perf_counter() - t0)
+        n = int(max(1e5, min(r0 * seconds, 5e8)))
     t0 = time.perf_counter()
     p.integrate(n, 0, threads)
     return n / (time.perf_counter() - t0), n, "port"
 
 
-def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
+def batched_section(args, ft, workloads, torch, flush, clocks_sampler, which):
     """The batched form: every integral of a seeded batch in one CUDA graph launch per
     run (ft_batch_*), mixed precision against plain FP64 on the same integrals.
 
@@ -211,7 +216,7 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
         except ft.FeyntropError:
             return False
 
-    if args.batched == "scan":
+    if which == "scan":
         inputs, redrawn = workloads.box_pentagon_scan(args.batch_count or 4096, seed=3, accept=accept)
         name = ("box-pentagon kinematic scan: 4096 points (7 vertices, 8 edges, D=6, 3 eps orders), masses U[0,2], "
                 "invariants U[-10,10], lambda U[0.2,1], N log-uniform [1e5,1e7], Random(3)")
@@ -284,6 +289,11 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
                                 "includes": "host preprocessing of every integral, batch creation, one run"}
         b.close()
     out["mixed_over_fp64"] = rates["mixed"] / rates["plain_fp64"]
+    out["mixed_over_fp64_samples_per_run"] = {"mixed": out["mixed"]["samples_per_run"],
+                                              "plain_fp64": out["plain_fp64"]["samples_per_run"],
+                                              "note": "the FP64 arm runs every integral's N x %g (the rate does not "
+                                                      "depend on N while work items outnumber the GPU's block slots)"
+                                                      % args.batch_fp64_scale}
     # the CPU path on a bounded, evenly spaced subset of the same integrals
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -298,8 +308,18 @@ def batched_section(args, ft, workloads, torch, flush, clocks_sampler):
                                "sample": "integrals %s of the batch, %d samples in total, all host threads"
                                          % (pick, int(tot_n))}
         out["mixed_over_cpu"] = rates["mixed"] / out["cpu_baseline"]["value"]
-    # per-sample error of the mixed form against the FP64 form on the first 16 integrals
-    out["per_sample_error"] = sample_error(ft, plans[:16], 16 << 15)
+    # per-sample error of the mixed form against the FP64 form, per kernel class: its
+    # first four integrals in the batch's order, 32768 samples each
+    by_class = {}
+    for p, x in zip(plans, inputs):
+        cls = "E%d V%d K%d %s" % (p.E, p.V, p.K, "deformed" if p.info["deformed"] else "undeformed")
+        if len(by_class.setdefault(cls, [])) < 4:
+            by_class[cls].append(p)
+    out["per_sample_error"] = {cls: sample_error(ft, ps, len(ps) << 15) for cls, ps in sorted(by_class.items())}
+    worst = max(by_class, key=lambda c: out["per_sample_error"][c]["max"])
+    out["per_sample_error_max"] = {"class": worst, "max": out["per_sample_error"][worst]["max"],
+                                   "frac_above_1e-5": max(v["frac_above_1e-5"]
+                                                          for v in out["per_sample_error"].values())}
     for p in plans:
         p.close()
     return out
@@ -331,13 +351,12 @@ def configs_section(args, ft, workloads, torch, flush):
     L2 flushed between them), mixed and plain FP64:
       K4:   complete graph K4, Euclidean, masses 0..5, 3 eps orders, N = 1e7;
       cube: 5-loop 2-point cube graph (8 vertices, 12 edges), Euclidean, 4 eps orders,
-            N = 1e9 mixed (plain FP64 on 1e8 of the same stream: the rate does not
-            depend on N at these sizes)."""
+            N = 1e9 in both forms."""
     stream = torch.cuda.Stream()
     fp32_peak, fp64_peak = device_peaks(ft)
     out = {}
     for name, inp, n_mixed, n_fp64 in (("K4", workloads.k4_euclidean(), 10 ** 7, 10 ** 7),
-                                      ("cube", workloads.cube_propagator(), 10 ** 9, 10 ** 8)):
+                                      ("cube", workloads.cube_propagator(), 10 ** 9, 10 ** 9)):
         plan = ft.Plan(inp)
         entry = {"workload": name, "samples_mixed": n_mixed, "samples_fp64": n_fp64}
         for prec, n, tag in ((ft.MIXED, n_mixed, "mixed"), (ft.FP64, n_fp64, "plain_fp64")):
@@ -399,22 +418,26 @@ def run_reference(args):
     from feyntrop_gb300 import workloads
     inp = workloads.double_box(N=args.samples)
     threads = os.cpu_count() or 1
-    vals = []
-    kind = None
-    nsample = 0
-    for step in range(args.warmup + args.steps):
-        v, nsample, kind = cpu_rate(inp, args.ref_seconds, threads)
-        if step >= args.warmup:
-            vals.append(v)
-    value = sum(vals) / len(vals)
+    # the first warm-up step sizes the per-step sample (about --ref-seconds of CPU work);
+    # every later step runs exactly that many samples, and a step's time is theirs
+    _, nsample, kind = cpu_rate(inp, args.ref_seconds, threads)
+    secs = []
+    for step in range(max(0, args.warmup - 1) + args.steps):
+        v, _, kind = cpu_rate(inp, args.ref_seconds, threads, n=nsample)
+        if step >= max(0, args.warmup - 1):
+            secs.append(nsample / v)
+    value = nsample * len(secs) / sum(secs)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": args.samples / value * 1e3, "higher_is_better": True,
+        "warmup": args.warmup, "ms_per_step": sum(secs) / len(secs) * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded double-box kinematics)",
-        "config": {"workload": "double box, Minkowski, lambda=0.5, 2 eps orders, N=%d per step" % args.samples,
+        "config": {"workload": "double box, Minkowski, lambda=0.5, 2 eps orders, N=%d per step: a bounded sample "
+                               "(about %.0f s of all host cores) of the N=%d workload, the same stream"
+                               % (nsample, args.ref_seconds, args.samples),
                    "host_threads": threads},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": "%d samples of the same stream per step, rate extrapolated to N" % nsample},
+                         "sample": "%d samples of the double-box stream per step (seed 0, samples [0, N))"
+                                   % nsample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -432,8 +455,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--kernel-only", action="store_true",
                     help="only the timed sampling steps (for profiler captures); prints a reduced line")
-    ap.add_argument("--batched", default="scan", choices=["scan", "mixed", "none"],
-                    help="the batched form's workload (one GPU runs it, rank 0 reports it)")
+    ap.add_argument("--workload", default="double_box", choices=["double_box", "cube", "ladder_mink", "box_pentagon"],
+                    help="with --kernel-only: the integral of the timed steps (profiler captures of other classes)")
+    ap.add_argument("--batched", default="both", choices=["both", "scan", "mixed", "none"],
+                    help="the batched form's workloads (one GPU runs them, rank 0 reports them)")
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--no-configs", action="store_true", help="skip the K4 and cube configurations")
     ap.add_argument("--batch-count", type=int, default=0,
@@ -466,10 +491,30 @@ def main():
 
     if args.batch_only:
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-        print(json.dumps(batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local))), flush=True)
+        which = ["scan", "mixed"] if args.batched == "both" else [args.batched]
+        print(json.dumps({w: batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local), w)
+                          for w in which}), flush=True)
         return
     N = args.samples
-    inp = workloads.double_box(N=N)
+    if args.workload != "double_box" and not args.kernel_only:
+        raise SystemExit("--workload other than double_box needs --kernel-only (the headline is the double box)")
+    def accept(x):
+        try:
+            ft.subgraph_table(x)
+            return True
+        except ft.FeyntropError:
+            return False
+
+    if args.workload == "cube":
+        inp = workloads.cube_propagator(N=N)
+    elif args.workload == "ladder_mink":
+        # a Minkowski 3-loop ladder drawn as in the mixed batch (Random(5): masses U[0, 3],
+        # s U[8, 20], t U[-6, -1], lambda 0.5; the second ladder drawn, the first Minkowski one)
+        inp = [x for x in workloads.mixed_batch(seed=5, counts=(0, 2, 0, 0), accept=accept)[0] if x["lambda"] != 0][0]
+    elif args.workload == "box_pentagon":
+        inp = workloads.box_pentagon_scan(1, seed=3, accept=accept)[0][0]
+    else:
+        inp = workloads.double_box(N=N)
     plan = ft.Plan(inp)
     stream = torch.cuda.Stream()
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -584,7 +629,9 @@ def main():
         pass
     batched = None
     if args.batched != "none" and rank == 0:
-        batched = batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local))
+        which = ["scan", "mixed"] if args.batched == "both" else [args.batched]
+        batched = {w: batched_section(args, ft, workloads, torch, flush, lambda: ClockSampler(local), w)
+                   for w in which}
     other = configs_section(args, ft, workloads, torch, flush) if (rank == 0 and not args.no_configs) else None
     lam = lambda_section(ft, workloads, 10 ** 8) if (rank == 0 and not args.no_configs) else None
     line = {

@@ -329,6 +329,25 @@ class Batch:
             out.append(r.as_dict(self.plans[i].info["IGtr"]))
         return out
 
+    def run_sharded(self, N, rank, world, seeds=0, first_samples=0, mode="samples", group=None, stream=None):
+        """The batch over `world` processes, one per GPU, every rank holding the same
+        batch (torch.distributed initialised, any backend): mode "samples" runs rank's
+        contiguous block of every integral's samples, mode "integrals" every world-th
+        integral whole (feyntrop_gb300.shard.batch_sharded).  The per-integral moments
+        of all ranks are gathered and merged; every rank returns, per integral,
+        {"integral", "moments", "samples"} of the whole batch."""
+        from . import shard
+        n = len(self.plans)
+        Ns = [int(x) for x in N] if hasattr(N, "__len__") else [int(N)] * n
+
+        def run(mine, seeds_, firsts):
+            return self.run([m or 0 for m in mine], seeds=seeds_, first_samples=firsts, stream=stream)
+
+        integrals, moments = shard.batch_sharded(run, Ns, [p.K for p in self.plans],
+                                                 [not p.info["deformed"] for p in self.plans], rank, world,
+                                                 seeds=seeds, first_samples=first_samples, mode=mode, group=group)
+        return [{"integral": i, "moments": m, "samples": Ns[k]} for k, (i, m) in enumerate(zip(integrals, moments))]
+
     def run_to_accuracy(self, rel_target, pilot=100_000, max_samples=10**10, seeds=0, eps_order=0, stream=None):
         """Variance-adaptive sample counts: a pilot run of `pilot` samples per integral
         estimates each integral's per-sample spread; a second run continues every

@@ -90,13 +90,13 @@ struct ft_batch {
     std::vector<group> groups;
     std::vector<int> group_of, slot_of;     // per plan: class and position in it
     // run descriptors: [class headers][batch_inst records][item_prep records], copied in
-    size_t desc_bytes = 0, hdr_bytes = 0, out_doubles = 0, qacc_doubles = 0;
+    size_t desc_bytes = 0, hdr_bytes = 0, out_doubles = 0, qacc_words = 0;
     unsigned char* h_desc = nullptr;
     unsigned char* d_desc = nullptr;
     double* d_out = nullptr;     // per integral 8K+8 sums
     double* h_out = nullptr;
     class_header* h_hdr_out = nullptr;
-    double* d_qacc = nullptr;    // per integral 4K+4 FP64-pass sums
+    unsigned long long* d_qacc = nullptr;   // per integral the FP64 pass's exact accumulators (exact_words)
     cudaStream_t stream = nullptr;
     cudaEvent_t fork = nullptr, ev0 = nullptr, ev1 = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -253,8 +253,8 @@ void build(ft_batch& b)
         prep += nm * sizeof(item_prep);
         g.off_out = b.out_doubles;
         b.out_doubles += nm * (8 * g.K + 8);
-        g.off_qacc = b.qacc_doubles;
-        b.qacc_doubles += nm * (4 * g.K + 4);
+        g.off_qacc = b.qacc_words;
+        b.qacc_words += nm * ft::exact_words(g.K);
     }
     b.hdr_bytes = align_up(hdr, 64);
     const size_t inst_base = b.hdr_bytes, prep_base = inst_base + inst;
@@ -268,7 +268,7 @@ void build(ft_batch& b)
     cu(cudaMallocHost(&b.h_out, b.out_doubles * 8), "cudaMallocHost(batch results)");
     cu(cudaMallocHost(&b.h_hdr_out, b.hdr_bytes), "cudaMallocHost(batch counters)");
     cu(cudaMalloc(&b.d_out, b.out_doubles * 8), "cudaMalloc(batch results)");
-    if (prec) cu(cudaMalloc(&b.d_qacc, b.qacc_doubles * 8), "cudaMalloc(batch FP64-pass sums)");
+    if (prec) cu(cudaMalloc(&b.d_qacc, b.qacc_words * 8), "cudaMalloc(batch FP64-pass sums)");
     std::memset(b.h_desc, 0, b.desc_bytes);
     // static parts of the instance records
     for (ft_batch::group& g : b.groups)
@@ -289,7 +289,7 @@ void record(ft_batch& b)
 {
     cudaStream_t s = b.stream;
     cu(cudaMemcpyAsync(b.d_desc, b.h_desc, b.desc_bytes, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(descriptors)");
-    if (b.precision) cu(cudaMemsetAsync(b.d_qacc, 0, b.qacc_doubles * 8, s), "cudaMemsetAsync");
+    if (b.precision) cu(cudaMemsetAsync(b.d_qacc, 0, b.qacc_words * 8, s), "cudaMemsetAsync");
     const device_state& ds = dev_state();
     b.launches = 0;
     for (ft_batch::group& g : b.groups) {
@@ -320,7 +320,7 @@ void record(ft_batch& b)
                                          (CUstream)g.stream, args, nullptr),
                   "launch ft_sample_batch");
         b.launches++;
-        double* qacc = nullptr;
+        unsigned long long* qacc = nullptr;
         if (b.precision) {
             qacc = b.d_qacc + g.off_qacc;
             const unsigned long long* cq = g.d_queue;

@@ -1,4 +1,5 @@
 #include "jit.hpp"
+#include "kernels/aot.hpp"
 
 #include <cuda_runtime.h>
 #include <dlfcn.h>
@@ -32,16 +33,14 @@ unsigned table_smem_bytes(const kernel_key& k)
     const unsigned tab = k.table_global ? 0u : (k.prec == 0 ? 25u * entries : 17u * entries);
     const unsigned parts = k.mode == 1 ? 4u : 2u;
     const unsigned acc = (unsigned)k.block * parts * (unsigned)k.K * (k.prec == 0 ? 16u : 24u);
-    // the V pass buffer (mixed deformed kernels with variant bits 2 and 3)
-    const unsigned vbuf =
-        (k.prec == 1 && k.mode == 1 && (k.variant & 12) == 12) ? 16u + 2u * (unsigned)k.block * 40u : 0u;
-    return ((tab + 15u) & ~15u) + acc + vbuf;
+    return ((tab + 15u) & ~15u) + acc;
 }
 
-// Tables of the two-float logarithm and exponential of the mixed kernels (FP32 values
-// written exactly as hexadecimal literals):
+// Tables of the two-float logarithm, exponential and sine / cosine of the mixed kernels
+// (FP32 values written exactly as hexadecimal literals):
 //   FT_LOGTAB[3i .. 3i+2] = r_i = fl(1 / (1 + (i + 1/2)/64)), -log(r_i) as hi, lo (i < 64)
 //   FT_EXPTAB[2j .. 2j+1] = 2^(j/32) as hi, lo (j < 32)
+//   FT_SCTAB[4j .. 4j+3]  = sin(j pi/64) as hi, lo, cos(j pi/64) as hi, lo (j < 128)
 static std::string tables_source()
 {
     static const std::string text = [] {
@@ -66,6 +65,18 @@ static std::string tables_source()
                 s << buf;
             }
         }
+        s << "};\n__device__ const float4 FT_SCTAB[128] = {";
+        const double pi = 3.14159265358979323846;
+        for (int j = 0; j < 128; j++) {
+            const double sn = std::sin(j * pi / 64.0), cs = std::cos(j * pi / 64.0);
+            const float sh = (float)sn, sl = (float)(sn - (double)sh), ch = (float)cs, cl = (float)(cs - (double)ch);
+            s << "{";
+            for (float v : {sh, sl, ch, cl}) {
+                std::snprintf(buf, sizeof buf, "%af,", (double)v);
+                s << buf;
+            }
+            s << "},";
+        }
         s << "};\n";
         return s.str();
     }();
@@ -82,7 +93,8 @@ std::string kernel_source(const kernel_key& k)
     s << "#define FT_ONLY_PSI " << k.only_psi << "\n#define FT_RECORD " << k.record << "\n";
     s << "#define FT_BLOCK " << k.block << "\n#define FT_TABLE_GLOBAL " << k.table_global << "\n";
     s << "#define FT_MINB " << k.minb << "\n#define FT_VARIANT " << k.variant << "\n";
-    s << "#define FT_BATCH " << k.batch << "\n";
+    s << "#define FT_BATCH " << k.batch << "\n#define FT_XA_DIGITS " << kExactDigits << "\n";
+    s << "#define FT_Q0 " << k.q0 << "\n";
     s << "__device__ constexpr int FT_EK[" << k.E << "] = {";
     for (int e = 0; e < k.E; e++) s << (e ? "," : "") << k.ek[e];
     s << "};\n__device__ constexpr int FT_EL[" << k.E << "] = {";
@@ -256,7 +268,7 @@ static std::string key_string(const kernel_key& k)
     std::ostringstream s;
     s << k.E << "," << k.V << "," << k.K << "," << k.loops << "," << k.rank << "," << k.prec << "," << k.mode << ","
       << k.only_psi << "," << k.record << "," << k.block << "," << k.table_global << "," << k.minb << "," << k.variant
-      << "," << k.batch;
+      << "," << k.batch << "," << k.q0;
     for (int e = 0; e < k.E; e++) s << ";" << k.ek[e] << "-" << k.el[e];
     return s.str();
 }

@@ -25,7 +25,8 @@ struct kernel_key {
     int minb = 1;           // minimum resident blocks per SM asked of the register allocator
     int variant = 0;        // code-size options of the kernel body (FT_VARIANT)
     int batch = 0;          // 1: the batch kernels (many integrals of the topology per launch)
-    std::vector<int> ek, el;
+    int q0 = 0;             // reduced vertices [0, q0) carry no external momentum (zero rows of P~)
+    std::vector<int> ek, el;   // endpoints in the kernel's vertex labels, ek > el
 };
 
 struct kernel_set {

@@ -210,14 +210,49 @@ __global__ void __launch_bounds__(128) ft_warp_states(const u64* __restrict__ la
     if (lane < 4) out[(size_t)w * 4 + lane] = word_of(g, lane);
 }
 
-// Per instance: the sums of its work items (double-double for the moment pairs) plus
-// the FP64 pass's sums (qacc, NULL for FP64 batches).  One thread per (instance,
-// moment pair or counter).  Slots: 8K moments as 4K (hi, lo) pairs, then kept,
-// dropped, queued, exact, robust, 3 spare; qacc: 4K sums, kept, dropped, robust, spare.
-__global__ void ft_batch_finalize(const batch_inst_view* __restrict__ inst, int n, const double* __restrict__ parts,
-                                  int K, const double* __restrict__ qacc, double* __restrict__ out)
+// An exact fixed-point accumulator (kExactDigits signed 64-bit digits of weight
+// 2^(32 j - 1074)) as a double-double: carries normalised from the lowest digit up
+// (digits in [0, 2^32), the sign in the final carry), a negative total negated, then
+// the digits added from the most significant down.
+__device__ void exact_to_dd(const u64* __restrict__ dig, double& h, double& l)
 {
-    const int slots = 8 * K + 8, units = 4 * K + 8, qslots = 4 * K + 4;
+    unsigned int d[ft::kExactDigits];
+    long long carry = 0;
+    for (int j = 0; j < ft::kExactDigits; j++) {
+        const long long t = (long long)dig[j] + carry;
+        d[j] = (unsigned int)(unsigned long long)t;
+        carry = t >> 32;
+    }
+    const bool neg = carry < 0;
+    if (neg) {
+        // two's complement of the digit vector: invert, add one
+        unsigned long long c = 1;
+        for (int j = 0; j < ft::kExactDigits; j++) {
+            const unsigned long long t = (unsigned long long)(~d[j]) + c;
+            d[j] = (unsigned int)t;
+            c = t >> 32;
+        }
+    }
+    h = 0.0;
+    l = 0.0;
+    for (int j = ft::kExactDigits - 1; j >= 0; j--)
+        if (d[j]) dd_add(h, l, ldexp((double)d[j], 32 * j - 1074), 0.0);
+    if (neg) {
+        h = -h;
+        l = -l;
+    }
+}
+
+// Per instance: the sums of its work items (double-double for the moment pairs) plus
+// the FP64 pass's exact sums (qacc, NULL for FP64 batches).  One thread per (instance,
+// moment pair or counter).  Slots: 8K moments as 4K (hi, lo) pairs, then kept,
+// dropped, queued, exact, robust, 3 spare; qacc: 4K exact accumulators, then kept,
+// dropped, robust, spare.
+__global__ void ft_batch_finalize(const batch_inst_view* __restrict__ inst, int n, const double* __restrict__ parts,
+                                  int K, const u64* __restrict__ qacc, double* __restrict__ out)
+{
+    const int slots = 8 * K + 8, units = 4 * K + 8;
+    const u64 qwords = 4ull * (u64)K * ft::kExactDigits + 4ull;   // ft::exact_words(K)
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)n * units) return;
     const int m = (int)(t / units), u = (int)(t % units);
@@ -227,7 +262,11 @@ __global__ void ft_batch_finalize(const batch_inst_view* __restrict__ inst, int 
         double h = 0.0, l = 0.0;
         for (u64 k = 0; k < cnt; k++)
             dd_add(h, l, parts[(f + k) * slots + 2 * u], parts[(f + k) * slots + 2 * u + 1]);
-        if (qacc) dd_add(h, l, qacc[(size_t)m * qslots + u], 0.0);
+        if (qacc) {
+            double qh, ql;
+            exact_to_dd(qacc + (size_t)m * qwords + (size_t)u * ft::kExactDigits, qh, ql);
+            dd_add(h, l, qh, ql);
+        }
         o[2 * u] = h;
         o[2 * u + 1] = l;
     } else {
@@ -235,9 +274,10 @@ __global__ void ft_batch_finalize(const batch_inst_view* __restrict__ inst, int 
         double v = 0.0;
         for (u64 k = 0; k < cnt; k++) v += parts[(f + k) * slots + 8 * K + c];
         if (qacc) {
-            if (c == 0) v += qacc[(size_t)m * qslots + 4 * K];
-            if (c == 1) v += qacc[(size_t)m * qslots + 4 * K + 1];
-            if (c == 4) v += qacc[(size_t)m * qslots + 4 * K + 2];
+            const u64* cnt4 = qacc + (size_t)m * qwords + 4ull * K * ft::kExactDigits;
+            if (c == 0) v += (double)cnt4[0];
+            if (c == 1) v += (double)cnt4[1];
+            if (c == 4) v += (double)cnt4[2];
         }
         o[8 * K + c] = v;
     }
@@ -303,9 +343,22 @@ double fma_peak_tflops(bool fp64)
 // library, held until the process exits:
 //   [2 words] FP64 hand-off queue count, [NOALLOC_PART_DOUBLES] per-block partial
 //   moments, [5 * NOALLOC_QUEUE_ENTRIES] hand-off queue, [NOALLOC_LANE_WORDS] lane
-//   skip matrices.
+//   skip matrices, [NOALLOC_WARP_WORDS] warp start states.
 // Every call shares it (and it keeps the last call's contents), so calls that overlap
 // on the GPU race; the queue count is cleared at the start of each call.
+constexpr unsigned long long kNoallocParts = 2, kNoallocQueue = kNoallocParts + NOALLOC_PART_DOUBLES,
+                             kNoallocLanes = kNoallocQueue + 5ull * NOALLOC_QUEUE_ENTRIES,
+                             kNoallocWarps = kNoallocLanes + NOALLOC_LANE_WORDS;
+// the regions end inside the array, and each holds what the host-side checks of
+// ft_integrate_noalloc let a call use: 2048 blocks of up to 8K+8 = 136 slots (16 eps
+// orders), the stream states of every warp of 2048 blocks of up to 1024 threads, the
+// 1024-word skip matrices of up to 24 lane bits
+static_assert(kNoallocWarps + NOALLOC_WARP_WORDS <= NOALLOC_TOTAL_WORDS, "no-allocation layout overruns");
+static_assert(NOALLOC_PART_DOUBLES >= NOALLOC_MAX_BLOCKS * (8 * 16 + 8), "partial sums of 16 eps orders");
+static_assert(NOALLOC_WARP_WORDS >= NOALLOC_MAX_BLOCKS * (1024 / 32) * 4, "warp states of 1024-thread blocks");
+static_assert(NOALLOC_LANE_WORDS >= NOALLOC_MAX_LANE_BITS * 1024, "lane skip matrices");
+static_assert(kNoallocQueue % 2 == 0 && kNoallocLanes % 2 == 0 && kNoallocWarps % 2 == 0,
+              "16-byte aligned regions (ulonglong2 loads)");
 static __device__ __align__(256) u64 g_noalloc_scratch[NOALLOC_TOTAL_WORDS];
 
 cudaError_t noalloc_scratch(noalloc_layout* out)
@@ -332,10 +385,10 @@ cudaError_t noalloc_scratch(noalloc_layout* out)
     }
     u64* w = (u64*)base;
     out->qcount = (unsigned int*)w;
-    out->parts = (double*)(w + 2);
-    out->queue = w + 2 + NOALLOC_PART_DOUBLES;
-    out->lanepw = w + 2 + NOALLOC_PART_DOUBLES + 5 * (size_t)NOALLOC_QUEUE_ENTRIES;
-    out->warpst = out->lanepw + NOALLOC_LANE_WORDS;
+    out->parts = (double*)(w + kNoallocParts);
+    out->queue = w + kNoallocQueue;
+    out->lanepw = w + kNoallocLanes;
+    out->warpst = w + kNoallocWarps;
     return cudaSuccess;
 }
 
@@ -353,8 +406,8 @@ cudaError_t launch_batch_item_states(const void* prep, int n, const u64* tpow, c
     return cudaGetLastError();
 }
 
-cudaError_t launch_batch_finalize(const void* inst, int n, const double* parts, int K, const double* qacc,
-                                  double* out, cudaStream_t st)
+cudaError_t launch_batch_finalize(const void* inst, int n, const double* parts, int K,
+                                  const unsigned long long* qacc, double* out, cudaStream_t st)
 {
     if (n <= 0) return cudaSuccess;
     const long long threads = (long long)n * (4 * K + 8);

@@ -14,8 +14,17 @@ cudaError_t launch_lane_powers(const unsigned long long* tpow, unsigned long lon
 // pass (qacc may be NULL).
 cudaError_t launch_batch_item_states(const void* prep, int n, const unsigned long long* tpow,
                                      const unsigned long long* itemM, unsigned long long* out, cudaStream_t st);
-cudaError_t launch_batch_finalize(const void* inst, int n, const double* parts, int K, const double* qacc,
-                                  double* out, cudaStream_t st);
+cudaError_t launch_batch_finalize(const void* inst, int n, const double* parts, int K,
+                                  const unsigned long long* qacc, double* out, cudaStream_t st);
+
+// The FP64 pass of a mixed batch adds each handed-off sample's values exactly into
+// per-integral fixed-point accumulators: digit j (a signed 64-bit counter) has weight
+// 2^(32 j - 1074), and a double enters as three signed 32-bit digits of its integer
+// significand, so the sums are exact and independent of the order of the atomics.
+// Per integral: 4K accumulators of kExactDigits words, then 4 counters (kept,
+// dropped, robust, spare).  The kernel source gets the same count as FT_XA_DIGITS.
+constexpr int kExactDigits = 68;
+inline unsigned long long exact_words(int K) { return 4ull * (unsigned long long)K * kExactDigits + 4ull; }
 
 // out[s] = sum over parts of parts[p * slots + s]; slots [0, ndd) are (hi, lo) pairs
 cudaError_t launch_finalize(const double* parts, int nparts, int slots, int ndd, double* out, cudaStream_t st);

@@ -65,8 +65,8 @@ typedef unsigned int u32;
 // transcendental, bit 1 does the same for the two-float primitives, so the code the
 // SM streams per sample fits the instruction caches better; bit 2 starts every sample
 // with a block-wide barrier, so that the block's warps walk the code together and
-// share its instruction fetches; bit 3 (with bit 2, deformed mixed kernels) adds the
-// V pass below.
+// share its instruction fetches; bit 3 keeps one out-of-line copy of each larger
+// two-float routine (logarithm, exponential, e^(ix), complex inverse, argument).
 #ifndef FT_VARIANT
 #define FT_VARIANT 0
 #endif
@@ -80,6 +80,11 @@ typedef unsigned int u32;
 #else
 #define FT_DFFN __forceinline__
 #endif
+#if (FT_VARIANT & 8) && !defined(FT_HOST_SIM)
+#define FT_BIGFN __noinline__
+#else
+#define FT_BIGFN __forceinline__
+#endif
 static __device__ FT_MATHFN float m_log1p(float x) { return log1pf(x); }
 static __device__ FT_MATHFN float m_exp(float x) { return expf(x); }
 static __device__ FT_MATHFN float m_exp2(float x) { return exp2f(x); }
@@ -87,8 +92,15 @@ static __device__ FT_MATHFN float m_log2(float x) { return log2f(x); }
 static __device__ FT_MATHFN float m_atan2(float y, float x) { return atan2f(y, x); }
 static __device__ FT_MATHFN float m_hypot(float x, float y) { return hypotf(x, y); }
 static __device__ FT_MATHFN void m_sincos(float x, float* s, float* c) { sincosf(x, s, c); }
+static __device__ FT_MATHFN float m_atan(float x) { return atanf(x); }
 
 #define FT_N (FT_V - 1)
+// reduced vertices [0, FT_Q0) carry no external momentum: the vectors q_r of P~ vanish
+// there (the host labels the internal vertices first), so the forward substitutions
+// of the quadratic forms start at row FT_Q0
+#ifndef FT_Q0
+#define FT_Q0 0
+#endif
 #define FT_FULL ((1u << FT_E) - 1u)
 #define FT_NPAIR (FT_E * (FT_E - 1) / 2)
 
@@ -138,16 +150,6 @@ static __device__ FT_MATHFN void m_sincos(float x, float* s, float* c) { sincosf
 #define REC_QUEUED 2
 #define REC_EXACT 4
 #define REC_ROBUST 8
-#define REC_VPASS 16
-// V pass (FT_VARIANT bit 3, with the per-sample barrier, deformed mixed kernels):
-// samples rejected only for the FP32 rounding of V are collected per block in shared
-// memory and re-evaluated, all threads of the block together, with V in two-float
-#if FT_PREC == 1 && FT_MODE == 1 && (FT_VARIANT & 12) == 12
-#define FT_VPASS 1
-#else
-#define FT_VPASS 0
-#endif
-#define ACC_VPASS (8 * FT_K + 5)
 
 // ------------------------------------------------------------------ small helpers
 static __device__ __forceinline__ u64 rotl64(u64 x, int k) { return (x << k) | (x >> (64 - k)); }
@@ -290,17 +292,18 @@ struct elim {
         return worst;
     }
 
-    // q^T L^{-1} q for a real vector q (forward substitution y = M^-T q, sum y^2/d)
+    // q^T L^{-1} q for a real vector q (forward substitution y = M^-T q, sum y^2/d;
+    // y vanishes on the rows before FT_Q0, where q does)
     template <class Q>
     __device__ __forceinline__ F quad(const Q* q) const
     {
         F y[FT_N];
         F s = F{};
 #pragma unroll
-        for (int i = 0; i < FT_N; i++) {
+        for (int i = FT_Q0; i < FT_N; i++) {
             F yi = from_real((R)q[i]);
 #pragma unroll
-            for (int k = 0; k < i; k++) yi = yi + a[k][i] * y[k];
+            for (int k = FT_Q0; k < i; k++) yi = yi + a[k][i] * y[k];
             y[i] = yi;
             s = s + yi * yi * inv_of(d[i]);
         }
@@ -314,10 +317,10 @@ struct elim {
         F y[FT_N];
         F s = F{};
 #pragma unroll
-        for (int i = 0; i < FT_N; i++) {
+        for (int i = FT_Q0; i < FT_N; i++) {
             F yi = from_real((R)q[i]);
 #pragma unroll
-            for (int k = 0; k < i; k++) yi = yi + a[k][i] * y[k];
+            for (int k = FT_Q0; k < i; k++) yi = yi + a[k][i] * y[k];
             y[i] = yi;
             const F t = yi * yi * inv_of(d[i]);
             s = s + t;
@@ -732,7 +735,7 @@ static __device__ __forceinline__ f2 f2_two_sum(float a, float b)
 // r_i = fl(1/c_i) and -log r_i (two-float) from FT_LOGTAB; z = M r_i - 1 (|z| < 1/100)
 // from exact products, log M = -log r_i + log1p(z) with log1p(z) = z - z^2/2 + z^3/3 -
 // z^4/4 + z^5/5, the terms past z in FP32.
-static __device__ __forceinline__ f2 log1m_u2(u64 x)
+static __device__ FT_BIGFN f2 log1m_u2(u64 x)
 {
     const u64 q = (1ull << 53) - (x >> 11);   // 1 .. 2^53
     const int lz = __clzll(q);
@@ -762,7 +765,7 @@ static __device__ __forceinline__ f2 log1m_u2(u64 x)
 // e^a = 2^m 2^(j/32) e^s, 2^(j/32) as two floats from FT_EXPTAB, e^s = 1 + s + s^2/2 +
 // s^3/6 + s^4/24 with the terms past s in FP32.  ln2/32 = C1 + C2 + C3, C1 with 11
 // significant bits so that k C1 is exact for |k| < 2^13.
-static __device__ __forceinline__ f2 exp_f2(f2 a)
+static __device__ FT_BIGFN f2 exp_f2(f2 a)
 {
     const float C1 = 0x1.62cp-6f, C2 = 0x1.217f7ep-17f, C3 = -0x1.c610cap-42f;
     const float kf = rintf(a.hi * 46.1662407f);
@@ -979,7 +982,7 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
         for (int i = 0; i < FT_N; i++) {
             double s = 0.0;
 #pragma unroll
-            for (int j = 0; j < FT_N; j++) s += G[i][j] * prm[P_Q + r * FT_N + j];
+            for (int j = FT_Q0; j < FT_N; j++) s += G[i][j] * prm[P_Q + r * FT_N + j];
             h[i] = s;
         }
 #pragma unroll
@@ -1183,14 +1186,13 @@ static __device__ __forceinline__ df df_of(f2 x)
     return r;
 }
 
-#if FT_VPASS
-// ------------------------------------------------------------------ V in two-float (V pass)
-// Complex two-float numbers, and sin / cos of a two-float angle to ~1e-14: the angle is
-// reduced by the nearest multiple k of pi/2 (pi/2 as a three-part constant, each k * part
-// formed exactly with an FMA), then sin and cos of the reduced r in [-pi/4, pi/4] come
-// from their Taylor series, r (1 - z/3! + z^2/5! - ...) and 1 - z/2! + z^2/4! - ...
-// with z = r^2, summed by Horner's rule in two-float (coefficients 1/n! as float pairs;
-// the series is cut where z^k/n! < 1e-16).
+// ------------------------------------------------------------------ complex two-float
+// Complex two-float numbers, and sin / cos of a two-float angle to ~1e-13, table-driven
+// after Tang: x = k pi/64 + r with |r| <= pi/128 (pi/64 as three FP32 parts, each
+// k * part formed exactly with an FMA); sin(k pi/64), cos(k pi/64) as float pairs from
+// FT_SCTAB (k mod 128); sin r = r - r^3/6 + r^5/120 and cos r = 1 - r^2/2 + r^4/24 -
+// r^6/720 with r and r^2 in two-float and the terms below 3e-6 in FP32; then
+// sin x = sin a cos r + cos a sin r, cos x = cos a cos r - sin a sin r in two-float.
 struct cdf {
     df re, im;
 };
@@ -1209,70 +1211,79 @@ static __device__ __forceinline__ cdf operator*(cdf a, cdf b)
     return cdf_mk(df_fma(a.re, b.re, df_neg(df_mul(a.im, b.im))), df_fma(a.re, b.im, df_mul(a.im, b.re)));
 }
 static __device__ __forceinline__ cdf operator*(df s, cdf a) { return cdf_mk(df_mul(s, a.re), df_mul(s, a.im)); }
-static __device__ __forceinline__ cdf cdf_inv(cdf a)
+static __device__ FT_BIGFN cdf cdf_inv(cdf a)
 {
     const df m = df_inv(df_fma(a.re, a.re, df_mul(a.im, a.im)));
     return cdf_mk(df_mul(a.re, m), df_neg(df_mul(a.im, m)));
 }
-
-static __device__ __forceinline__ void sincos_df(df x, df& s, df& c)
+// a b + c with four two-float FMAs
+static __device__ __forceinline__ cdf cdf_fma(cdf a, cdf b, cdf c)
 {
-    const float P1 = 0x1.921fb6p+0f, P2 = -0x1.777a5cp-25f, P3 = -0x1.ee59dap-50f;
-    const float k = rintf((x.hi + x.lo) * 0x1.45f306p-1f);
+    return cdf_mk(df_fma(a.re, b.re, df_fma(df_neg(a.im), b.im, c.re)), df_fma(a.re, b.im, df_fma(a.im, b.re, c.im)));
+}
+// z 2^-k for the exponent k of z's larger part (exact), the exponent added to k_acc;
+// false when z is zero or not finite
+static __device__ __forceinline__ bool cdf_renorm(cdf& z, int& k_acc)
+{
+    const float mx = fmaxf(fabsf(z.re.hi), fabsf(z.im.hi));
+    const int be = (__float_as_int(mx) >> 23) & 0xff;
+    const bool ok = be > 0 && be < 255;
+    const int k = ok ? be - 127 : 0;
+    const float sc = __int_as_float((127 - k) << 23);
+    z.re.hi *= sc;
+    z.re.lo *= sc;
+    z.im.hi *= sc;
+    z.im.lo *= sc;
+    k_acc += k;
+    return ok;
+}
+
+// e^(ix) = cos x + i sin x
+static __device__ FT_BIGFN cdf expi_df(df x)
+{
+    const float P1 = 0x1.921fb6p-5f, P2 = -0x1.777a5cp-30f, P3 = -0x1.ee59dap-55f;
+    const float k = rintf((x.hi + x.lo) * 0x1.45f306p+4f);
     const float p1 = k * P1, e1 = fmaf(k, P1, -p1);
     const float p2 = k * P2, e2 = fmaf(k, P2, -p2);
     df r = df_add(x, df_norm(-p1, -e1));
     r = df_add(r, df_norm(-p2, -e2));
     r = df_add(r, df_mk(-k * P3));
-    const df z = df_mul(r, r);
-    // (-1)^j / (2j+1)!, j = 0..7, and (-1)^j / (2j)!, j = 0..8, as (hi, lo)
-    const float SN[8][2] = {{1.0f, 0.0f},
-                            {-0x1.555556p-3f, 0x1.555556p-28f},
-                            {0x1.111112p-7f, -0x1.dddddep-32f},
-                            {-0x1.a01a02p-13f, 0x1.7f97fap-39f},
-                            {0x1.71de3ap-19f, 0x1.55b1ccp-45f},
-                            {-0x1.ae6456p-26f, -0x1.fd5138p-52f},
-                            {0x1.612462p-33f, -0x1.8af25ep-58f},
-                            {-0x1.ae7f3ep-41f, -0x1.ccee08p-67f}};
-    const float CS[9][2] = {{1.0f, 0.0f},
-                            {-0.5f, 0.0f},
-                            {0x1.555556p-5f, -0x1.555556p-30f},
-                            {-0x1.6c16c2p-10f, 0x1.27d27ep-35f},
-                            {0x1.a01a02p-16f, -0x1.7f97fap-42f},
-                            {-0x1.27e4fcp-22f, 0x1.10ec14p-47f},
-                            {0x1.1eed8ep-29f, 0x1.ff1b14p-54f},
-                            {-0x1.93974ap-37f, -0x1.180f94p-62f},
-                            {0x1.ae7f3ep-45f, 0x1.ccee08p-71f}};
-    df ps, pc;
-    ps.hi = SN[7][0];
-    ps.lo = SN[7][1];
-#pragma unroll
-    for (int j = 6; j >= 0; j--) {
-        df cj;
-        cj.hi = SN[j][0];
-        cj.lo = SN[j][1];
-        ps = df_fma(ps, z, cj);
-    }
-    pc.hi = CS[8][0];
-    pc.lo = CS[8][1];
-#pragma unroll
-    for (int j = 7; j >= 0; j--) {
-        df cj;
-        cj.hi = CS[j][0];
-        cj.lo = CS[j][1];
-        pc = df_fma(pc, z, cj);
-    }
-    const df sr = df_mul(r, ps);
-    const int q = ((int)k) & 3;
-    s = (q == 0) ? sr : (q == 1) ? pc : (q == 2) ? df_neg(sr) : df_neg(pc);
-    c = (q == 0) ? pc : (q == 1) ? df_neg(sr) : (q == 2) ? df_neg(pc) : sr;
+    const float rh = r.hi, r2 = rh * rh;
+    // sin r = r + rh^3 (-1/6 + rh^2/120)
+    const df sr = df_add(r, df_mk(rh * r2 * fmaf(r2, 0x1.111112p-7f, -0x1.555556p-3f)));
+    // cos r = 1 - (rh^2 + 2 rh r.lo)/2 + rh^4/24 - rh^6/720, with rh^2 = r2 + qe exactly
+    const float qe = fmaf(rh, rh, -r2);
+    const df cr = df_add(df_norm(1.0f, -0.5f * r2),
+                         df_mk(fmaf(-rh, r.lo, -0.5f * qe) + r2 * r2 * fmaf(r2, -0x1.6c16c2p-10f, 0x1.555556p-5f)));
+    const float4 t = FT_SCTAB[((int)k) & 127];
+    df sa, ca;
+    sa.hi = t.x;
+    sa.lo = t.y;
+    ca.hi = t.z;
+    ca.lo = t.w;
+    return cdf_mk(df_fma(ca, cr, df_neg(df_mul(sa, sr))), df_fma(sa, cr, df_mul(ca, sr)));
 }
 
-// V = -sum_r sigma_r q_r^T L(y)^-1 q_r + sum_e m2_e X_e e^(i theta_e) at the deformed point,
-// in two-float complex arithmetic: conductances y_e = e^(-i theta_e) / X_e from the
-// two-float contour and sector point, the same conductance-form elimination as `elim`,
-// the quadratic forms with sigma and q as two-float pairs.
-static __device__ __forceinline__ cdf v_twofloat(const df* theta, const f2* Xi2, const float* pd)
+// The deformed Laplacian at the sample (srcs/feynman_integral.hpp:293-310) and V there
+// (:322-336) in two-float complex arithmetic, for every deformed sample: in FP32 both
+// suffer cancellation (the spanning-tree sum with phases, the quadratic forms against
+// the mass terms), and their errors enter the integrand as D/2 arg psi and W arg V.
+// Conductances y_e = e^(-i theta_e) / X_e from the two-float contour and sector point,
+// the conductance-form elimination of `elim`, the product of its pivots (rescaled by
+// powers of two as it goes: det L(y) = det * 2^det_e) and
+// V = -sum_r sigma_r q_r^T L(y)^-1 q_r + sum_e m2_e X_e e^(i theta_e).
+struct cblock {
+    cdf V;
+    cdf det;
+    int det_e;
+    bool ok;       // pivots and the determinant finite and non-zero
+    float growth;  // smallest pivot-to-row-size ratio of the elimination
+    float mag;     // sum of the magnitudes of V's terms
+    float qmag;    // the same through the forward substitutions: sum_r |sigma_r| sum_i |y_i^2 / d_i| + masses
+};
+static __device__ __forceinline__ float cmag_hi(const cdf& z) { return fabsf(z.re.hi) + fabsf(z.im.hi); }
+
+static __device__ __forceinline__ void complex_block(const df* theta, const f2* Xi2, const float* pd, cblock& o)
 {
     auto pdf = [&](int i) -> df {
         df v;
@@ -1280,17 +1291,6 @@ static __device__ __forceinline__ cdf v_twofloat(const df* theta, const f2* Xi2,
         v.lo = pd[2 * i + 1];
         return v;
     };
-    cdf y[FT_E];
-    cdf v = cdf_zero();
-#pragma unroll
-    for (int e = 0; e < FT_E; e++) {
-        df sn, cs;
-        sincos_df(theta[e], sn, cs);
-        const df xi = df_of(Xi2[e]);
-        y[e] = cdf_mk(df_mul(xi, cs), df_neg(df_mul(xi, sn)));
-        const df x = df_inv(xi);
-        v = v + pdf(P_M2 + e) * cdf_mk(df_mul(x, cs), df_mul(x, sn));
-    }
     cdf c[FT_N][FT_N], g[FT_N];
 #pragma unroll
     for (int i = 0; i < FT_N; i++) {
@@ -1298,47 +1298,79 @@ static __device__ __forceinline__ cdf v_twofloat(const df* theta, const f2* Xi2,
 #pragma unroll
         for (int j = 0; j < FT_N; j++) c[i][j] = cdf_zero();
     }
+    cdf v = cdf_zero();
+    float mag = 0.0f;
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
+        const cdf eix = expi_df(theta[e]);
+        const df cs = eix.re, sn = eix.im;
+        const df xi = df_of(Xi2[e]);
+        const cdf y = cdf_mk(df_mul(xi, cs), df_neg(df_mul(xi, sn)));
         const int k = FT_EK[e], l = FT_EL[e];
         if (k == FT_V - 1)
-            g[l] = g[l] + y[e];
+            g[l] = g[l] + y;
         else
-            c[l][k] = c[l][k] + y[e];
+            c[l][k] = c[l][k] + y;
+        const df m2x = df_mul(pdf(P_M2 + e), df_inv(xi));
+        v = v + cdf_mk(df_mul(m2x, cs), df_mul(m2x, sn));
+        mag += fabsf(m2x.hi);
     }
     cdf a[FT_N][FT_N], dinv[FT_N];
+    cdf det = cdf_mk(df_mk(1.0f), df_mk(0.0f));
+    int det_e = 0;
+    bool ok = true;
+    float worst = 1.0f;
 #pragma unroll
     for (int k = 0; k < FT_N; k++) {
         cdf dk = g[k];
+        float row = cmag_hi(g[k]);
 #pragma unroll
-        for (int j = k + 1; j < FT_N; j++) dk = dk + c[k][j];
+        for (int j = k + 1; j < FT_N; j++) {
+            dk = dk + c[k][j];
+            row += cmag_hi(c[k][j]);
+        }
+        worst = fminf(worst, cmag_hi(dk) / row);
+        det = det * dk;
+        ok &= cdf_renorm(det, det_e);
         dinv[k] = cdf_inv(dk);
 #pragma unroll
         for (int i = k + 1; i < FT_N; i++) a[k][i] = c[k][i] * dinv[k];
 #pragma unroll
         for (int i = k + 1; i < FT_N; i++) {
-            g[i] = g[i] + a[k][i] * g[k];
+            g[i] = cdf_fma(a[k][i], g[k], g[i]);
 #pragma unroll
-            for (int j = i + 1; j < FT_N; j++) c[i][j] = c[i][j] + a[k][i] * c[k][j];
+            for (int j = i + 1; j < FT_N; j++) c[i][j] = cdf_fma(a[k][i], c[k][j], c[i][j]);
         }
     }
+    float qmag = 0.0f;
 #pragma unroll
     for (int r = 0; r < FT_RANK; r++) {
         cdf yv[FT_N];
         cdf sr = cdf_zero();
+        float qm = 0.0f;
 #pragma unroll
-        for (int i = 0; i < FT_N; i++) {
+        for (int i = FT_Q0; i < FT_N; i++) {
             cdf yi = cdf_mk(pdf(P_Q + r * FT_N + i), df_mk(0.0f));
 #pragma unroll
-            for (int k = 0; k < i; k++) yi = yi + a[k][i] * yv[k];
+            for (int k = FT_Q0; k < i; k++) yi = cdf_fma(a[k][i], yv[k], yi);
             yv[i] = yi;
-            sr = sr + (yi * yi) * dinv[i];
+            const cdf t = (yi * yi) * dinv[i];
+            qm += cmag_hi(t);
+            sr = sr + t;
         }
-        v = v - pdf(P_SIG + r) * sr;
+        const df sg = pdf(P_SIG + r);
+        v = v - sg * sr;
+        mag += fabsf(sg.hi) * cmag_hi(sr);
+        qmag += fabsf(sg.hi) * qm;
     }
-    return v;
+    o.V = v;
+    o.det = det;
+    o.det_e = det_e;
+    o.ok = ok;
+    o.growth = worst;
+    o.mag = mag;
+    o.qmag = qmag + mag;
 }
-#endif
 
 // x-derivatives of phi/psi at the sample point (srcs/laplacian.hpp:102-215) and the
 // deformation angle theta = -lambda (d(phi/psi)/dx + m^2) (srcs/feynman_integral.hpp:290-291).
@@ -1414,7 +1446,7 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
         for (int i = 0; i < FT_N; i++) {
             df s = df_mk(0.0f);
 #pragma unroll
-            for (int j = 0; j < FT_N; j++) {
+            for (int j = FT_Q0; j < FT_N; j++) {
                 df q;
                 q.hi = pd[2 * (P_Q + r * FT_N + j)];
                 q.lo = pd[2 * (P_Q + r * FT_N + j) + 1];
@@ -1517,28 +1549,29 @@ static __device__ __forceinline__ f2 f2_mul2(f2 a, f2 b)
     return f2_make(h, e - (h - p));
 }
 static __device__ __forceinline__ f2 f2_neg(f2 a) { return f2_make(-a.hi, -a.lo); }
-// relative size of V below which the FP32 evaluation hands the sample to FP64
+// undeformed integrand: relative size of V below which the FP32 evaluation hands the
+// sample to FP64
 #ifndef V_CANCEL
 #define V_CANCEL 0.05f
 #endif
-// smallest pivot-to-row ratio accepted in the FP32 complex eliminations
+// smallest pivot-to-row ratio accepted in the FP32 elimination of the Jacobian
 #ifndef PIVOT_GROWTH
 #define PIVOT_GROWTH 0.02f
 #endif
-// largest accepted (D/2) det L(|y|) / |det L(y)|: the complex determinant is a sum over
-// spanning trees with phases, and FP32 errors in it (and in psi^(-D/2)) grow by the
-// ratio of the phase-free sum to the result
-#ifndef DET_CANCEL
-#define DET_CANCEL 400.0f
+// deformed integrand, the two-float complex block (det L(y) and V): smallest accepted
+// pivot-to-row ratio, smallest |V| relative to the sum of its terms' magnitudes, and
+// largest W qmag / |V| (qmag: the magnitudes of every term summed into V, through the
+// forward substitutions).  Two-float arithmetic keeps ~1e-14 of these magnitudes and
+// the sector point and contour it starts from ~1e-12, so the bounds only catch samples
+// whose cancellation would amplify that to ~1e-7.
+#ifndef ACC_GROWTH
+#define ACC_GROWTH 1e-5f
 #endif
-// largest accepted W qmag / |V| in the deformed integrand, qmag the magnitude of every
-// term summed into V (the forward substitutions' y_i^2 / d_i weighted by |sigma_r|, and
-// the mass terms): V^(-W) carries their FP32 rounding, amplified by the cancellation in
-// V.  At 120 the mixed form's samples stay within about 1.4e-5 of FP64 on random
-// box-pentagon kinematics with ~1 % handed off (the pivot-growth bound it replaces
-// let 0.02-0.03 % of the samples exceed 1e-5 at 0.7 %)
-#ifndef V_AMPLIFY
-#define V_AMPLIFY 120.0f
+#ifndef ACC_V_CANCEL
+#define ACC_V_CANCEL 1e-6f
+#endif
+#ifndef ACC_V_AMPLIFY
+#define ACC_V_AMPLIFY 1e5f
 #endif
 #define RLN2_HI 1.44269502162933349609375f
 #define RLN2_LO 1.925963033500011e-8f
@@ -1578,13 +1611,30 @@ static __device__ __forceinline__ f2 wrap_pi2(f2 x, bool& edge)
     return r;
 }
 
-// VX: V in two-float (the V pass); vfail reports a hand-off for V's rounding alone
-template <bool VX>
+// Principal argument of x + i y in two-float to about 1.5e-7 absolute: atanf of the
+// ratio of the smaller to the larger part (a result in [0, pi/4], where an ulp is
+// 6e-8), the octant restored with multiples of pi/2 in two-float, plus the first-order
+// effect of the low parts, (x dy - y dx) / |z|^2.  Zero gives 0.
+static __device__ FT_BIGFN f2 arg_f2(float x, float y, float xl, float yl)
+{
+    const float PIO2_HI = 1.57079637f, PIO2_LO = -4.37113883e-8f;
+    const float ax = fabsf(x), ay = fabsf(y);
+    const bool sw = ay > ax;
+    const float num = sw ? ax : ay, den = sw ? ay : ax;
+    const float a = den > 0.0f ? m_atan(num / den) : 0.0f;
+    f2 r = sw ? f2_add(f2_make(PIO2_HI, PIO2_LO), -a) : f2_make(a, 0.0f);
+    if (x < 0.0f) r = f2_add2(f2_make(2.0f * PIO2_HI, 2.0f * PIO2_LO), f2_neg(r));
+    if (y < 0.0f) r = f2_neg(r);
+    const float n2 = fmaf(x, x, y * y);
+    return n2 > 0.0f ? f2_add(r, (x * yl - y * xl) / n2) : r;
+}
+
+// Sets need64 when the FP32 / two-float evaluation cannot be trusted (the sample then
+// goes to the FP64 pass); returns false for a dropped (non-finite) sample.
 static __device__ __forceinline__ bool integrand32(const float* pd, const float* pf, const f2* lx, f2 lF, f2 lG,
-                                                   cx<float>* out, bool& need64, bool& vfail)
+                                                   cx<float>* out, bool& need64)
 {
     need64 = false;
-    vfail = false;
     const float D2 = 0.5f * pf[P_D], W = pf[P_W];
     // working frame X_e = exp(lx_e - sh), sh an integer near the middle of the range;
     // R and the eps factor are ratios to the tropical approximants and do not depend on it
@@ -1594,13 +1644,16 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     const float sh = rintf(0.5f * lmin);
     float X[FT_E], Xi[FT_E];
 #if FT_MODE == 1
-    // 1/X in two-float for the derivative block (theta is a function of X whose phase
-    // effect grows with |theta|); X and 1/X in FP32 from it
+    // 1/X in two-float for the derivative block and the complex Laplacian (theta is a
+    // function of X whose phase effect grows with |theta|); X and 1/X in FP32 from it;
+    // log prod X (in the frame) in two-float
     f2 Xi2[FT_E];
+    f2 sumlx = f2_make(0.0f, 0.0f);
     bool xbad = false;
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
         const f2 a = f2_add(lx[e], -sh);
+        sumlx = f2_add2(sumlx, a);
         Xi2[e] = exp_f2(f2_make(-a.hi, -a.lo));
         Xi[e] = Xi2[e].hi;
         X[e] = rcp_(Xi[e]);
@@ -1621,6 +1674,8 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
 #endif
     const f2 lFs = f2_add(lF, -(float)FT_LOOPS * sh);   // log psi_tr in the frame
     const f2 lGs = f2_add(lG, -sh);                      // log V_tr = log(xi_tr / psi_tr)
+    const float IGtr = pf[P_IGTR];
+#if FT_MODE == 0
     elim<float, float> L;
     L.factor(Xi);
     mexp psi = mx_one();
@@ -1632,8 +1687,6 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
         need64 = true;
         return false;
     }
-    const float IGtr = pf[P_IGTR];
-#if FT_MODE == 0
     const f2 lpsi = log2_ratio(psi, lFs);   // log2(psi / psi_tr)
 #if FT_ONLY_PSI
     const f2 t = f2_mulf(lpsi, -D2);
@@ -1683,7 +1736,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
 #else
     const float kappa = pf[P_DEF];
     // The contour (theta) and its Jacobian come from differences of entries of L^-1,
-    // which cancel in FP32 for a sizeable fraction of sectors; this block runs in FP64.
+    // which cancel in FP32 for a sizeable fraction of sectors; this block runs in two-float.
     df theta[FT_E];
     float H[FT_E][FT_E];
     bool cancel = false;
@@ -1692,156 +1745,120 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
         need64 = true;
         return false;
     }
-    cx<float> cX[FT_E], cy[FT_E];
+    // det(I + i kappa X^1/2 H X^1/2) (similar to I + i kappa H X, srcs/feynman_integral.hpp:312-320):
+    // the real part is the identity, so the symmetric elimination needs no pivoting; FP32,
+    // the pivots' product rescaled by powers of two (det J = pj 2^pj_e).  Before the complex
+    // block, so that H is no longer live there.
+    cx<float> pj = cmk(1.0f, 0.0f);
+    int pj_e = 0;
+    float jgrowth = 1.0f;
+    bool jok = true;
+    {
+        cx<float> J[FT_E][FT_E];
+        float sx[FT_E];
+#pragma unroll
+        for (int e = 0; e < FT_E; e++) sx[e] = sqrtf(X[e]);
+#pragma unroll
+        for (int a = 0; a < FT_E; a++)
+#pragma unroll
+            for (int b = a; b < FT_E; b++) J[a][b] = cmk(a == b ? 1.0f : 0.0f, kappa * H[a][b] * sx[a] * sx[b]);
+#pragma unroll
+        for (int k = 0; k < FT_E; k++) {
+            const cx<float> piv = J[k][k];
+            const float m = fabsf(piv.re) + fabsf(piv.im);
+            float row = m;
+#pragma unroll
+            for (int j = k + 1; j < FT_E; j++) row += fabsf(J[k][j].re) + fabsf(J[k][j].im);
+            jgrowth = fminf(jgrowth, m / row);
+            pj = pj * piv;
+            {
+                const float mx = fmaxf(fabsf(pj.re), fabsf(pj.im));
+                const int be = (__float_as_int(mx) >> 23) & 0xff;
+                jok &= be > 0 && be < 255;
+                const int kk = (be > 0 && be < 255) ? be - 127 : 0;
+                const float sc = __int_as_float((127 - kk) << 23);
+                pj = cmk(pj.re * sc, pj.im * sc);
+                pj_e += kk;
+            }
+            const cx<float> inv = crecip(piv);
+#pragma unroll
+            for (int i = k + 1; i < FT_E; i++) {
+                const cx<float> f = J[k][i] * inv;
+#pragma unroll
+                for (int j = i; j < FT_E; j++) J[i][j] = J[i][j] - f * J[k][j];
+            }
+        }
+    }
+    FT_DBG(29, jgrowth);
+    if (!jok || !(jgrowth > PIVOT_GROWTH)) {
+        need64 = true;
+        return false;
+    }
     // phase sums in two-float: sum theta and nu . theta
     f2 xnu = f2_make(0.0f, 0.0f), thsum = f2_make(0.0f, 0.0f);
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
         FT_DBG(e, theta[e].hi + theta[e].lo);
-        float sn, cs;
-        m_sincos(theta[e].hi, &sn, &cs);
-        // first-order correction for the low part: sin(h + l) = sin h + l cos h
-        const float cs2 = fmaf(-theta[e].lo, sn, cs), sn2 = fmaf(theta[e].lo, cs, sn);
-        cX[e] = cmk(X[e] * cs2, X[e] * sn2);
-        cy[e] = cmk(Xi[e] * cs2, -Xi[e] * sn2);   // 1 / cX
         thsum = f2_add2(thsum, f2_make(theta[e].hi, theta[e].lo));
         xnu = f2_add2(xnu, f2_mulf(f2_make(theta[e].hi, theta[e].lo), pf[P_NU + e]));
     }
-    elim<cx<float>, float> CL;
-    const float growth = CL.factor(cy);
-    // a pivot much smaller than the conductances summed into it loses ~1e-7 / growth
-    if (!(growth > PIVOT_GROWTH)) {
+    cblock cb;
+    complex_block(theta, Xi2, pd, cb);
+    FT_DBG(27, cb.growth);
+    // two-float pivots lose ~1e-14 / growth
+    if (!cb.ok || !(cb.growth > ACC_GROWTH)) {
         need64 = true;
         return false;
     }
-    // |cPsi| = prod X * prod |d_k|, arg cPsi = sum theta + sum arg d_k
-    mexp cpsi = mx_one();
-    cx<float> ph = cmk(1.0f, 0.0f);
-#pragma unroll
-    for (int e = 0; e < FT_E; e++) mx_mul(cpsi, X[e]);
-#pragma unroll
-    for (int k = 0; k < FT_N; k++) {
-        const float m = cabs_(CL.d[k]);
-        mx_mul(cpsi, m);
-        const float im = rcp_(m);
-        ph = ph * cmk(CL.d[k].re * im, CL.d[k].im * im);
+    // V = Vn 2^v_e, |Vn| in [1, 2 sqrt 2)
+    cdf Vn = cb.V;
+    int v_e = 0;
+    if (!cdf_renorm(Vn, v_e) || v_e > 126) {
+        need64 = true;
+        return false;
     }
-    {
-        const int de = min(max(psi.e - cpsi.e, -100), 100);
-        const float rho = psi.m / cpsi.m * __int_as_float((127 + de) << 23);
-        if (!(D2 * rho < DET_CANCEL)) {
-            need64 = true;
-            return false;
-        }
+    const float vsc = __int_as_float((127 - v_e) << 23);   // 2^-v_e
+    const float vn2 = fmaf(Vn.re.hi, Vn.re.hi, Vn.im.hi * Vn.im.hi);
+    const float vm = sqrtf(vn2);
+    FT_DBG(20, Vn.re.hi);
+    FT_DBG(21, Vn.im.hi);
+    FT_DBG(34, W * cb.qmag * vsc / vm);
+    // V in two-float keeps ~1e-14 of its terms' magnitudes (and ~1e-12 from the sector
+    // point and contour it is built from): samples where V cancels to below 1e-6 of its
+    // terms, or where W qmag / |V| exceeds 1e5, go to the FP64 pass
+    if (!(vm > ACC_V_CANCEL * (cb.mag * vsc)) || !(W * (cb.qmag * vsc) < ACC_V_AMPLIFY * vm)) {
+        need64 = true;
+        return false;
     }
     bool edge = false;
-    // arg cPsi = sum theta + arg det, reduced to the principal branch in two-float
-    const f2 apsi2 = wrap_pi2(f2_add(thsum, m_atan2(ph.im, ph.re)), edge);
-    const float apsi = apsi2.hi + apsi2.lo;
-    // phi/psi of the deformed point and the deformed V
-    cx<float> cpphi = cmk(0.0f, 0.0f);
-    float mag = 0.0f;
-    float qmag = 0.0f;   // magnitude of the terms summed into V, through the eliminations
-    cx<float> cV;
-#if FT_VPASS
-    if constexpr (VX) {
-        const cdf vd = v_twofloat(theta, Xi2, pd);
-        cV = cmk(vd.re.hi + vd.re.lo, vd.im.hi + vd.im.lo);
-    } else
-#endif
-    {
-#pragma unroll
-        for (int r = 0; r < FT_RANK; r++) {
-            float qm = 0.0f;
-            const cx<float> v = pf[P_SIG + r] * CL.quad_mag(pf + P_Q + r * FT_N, qm);
-            qmag += fabsf(pf[P_SIG + r]) * qm;
-            cpphi = cpphi - v;
-            mag += cabs_(v);
-        }
-        cV = cpphi;
-#pragma unroll
-        for (int e = 0; e < FT_E; e++) {
-            cV = cV + pf[P_M2 + e] * cX[e];
-            mag += pf[P_M2 + e] * X[e];
-        }
-        qmag += mag;
-    }
-    const float vabs = cabs_(cV);
-    FT_DBG(20, cV.re);
-    FT_DBG(21, cV.im);
-    FT_DBG(22, cpphi.re);
-    FT_DBG(23, cpphi.im);
-    // V cancels near thresholds: its FP32 error is ~ 1e-7 * mag / |V|, so samples where
-    // |V| < V_CANCEL * mag go to the FP64 pass.  The rounding inside the eliminations
-    // is bounded by the magnitudes of the terms they sum (qmag: sum_r |sigma_r|
-    // sum_i |y_i^2 / d_i| of the forward substitutions, plus the mass terms); V^-W
-    // turns it into a relative error of about 1e-7 W qmag / |V|.
-    if (!VX && (!(vabs > V_CANCEL * mag) || !(W * qmag < V_AMPLIFY * vabs))) {
-        need64 = true;
-        vfail = true;
-        return false;
-    }
-
-    mexp mv = mx_one();
-    mx_mul(mv, vabs);
-    const float av = m_atan2(cV.im, cV.re);
+    const f2 av2 = arg_f2(Vn.re.hi, Vn.im.hi, Vn.re.lo, Vn.im.lo);
+    const float av = av2.hi + av2.lo;
     edge |= fabsf(av) > 3.14158265f;
     FT_DBG(32, av);
-    FT_DBG(34, W * qmag / vabs);
     FT_DBG(33, xnu.hi + xnu.lo);
-    // det(I + i kappa X^1/2 H X^1/2)
-    cx<float> J[FT_E][FT_E];
-    float sx[FT_E];
-#pragma unroll
-    for (int e = 0; e < FT_E; e++) sx[e] = sqrtf(X[e]);
-#pragma unroll
-    for (int a = 0; a < FT_E; a++)
-#pragma unroll
-        for (int b = a; b < FT_E; b++) J[a][b] = cmk(a == b ? 1.0f : 0.0f, kappa * H[a][b] * sx[a] * sx[b]);
-    mexp mj = mx_one();
-    cx<float> pj = cmk(1.0f, 0.0f);
-    float jgrowth = 1.0f;
-#pragma unroll
-    for (int k = 0; k < FT_E; k++) {
-        const cx<float> piv = J[k][k];
-        const float m = cabs_(piv);
-        float row = m;
-#pragma unroll
-        for (int j = k + 1; j < FT_E; j++) row += fabsf(J[k][j].re) + fabsf(J[k][j].im);
-        jgrowth = fminf(jgrowth, m / row);
-        mx_mul(mj, m);
-        const float im = rcp_(m);
-        pj = pj * cmk(piv.re * im, piv.im * im);
-        const cx<float> inv = crecip(piv);
-#pragma unroll
-        for (int i = k + 1; i < FT_E; i++) {
-            const cx<float> f = J[k][i] * inv;
-#pragma unroll
-            for (int j = i; j < FT_E; j++) J[i][j] = J[i][j] - f * J[k][j];
-        }
-    }
-    FT_DBG(24, (float)mj.e + log2f(mj.m));
-    FT_DBG(25, atan2f(pj.im, pj.re));
+    // arg cPsi = sum theta + arg det L(y), reduced to the principal branch in two-float
+    const float dn2 = fmaf(cb.det.re.hi, cb.det.re.hi, cb.det.im.hi * cb.det.im.hi);
+    const f2 apsi2 = wrap_pi2(f2_add2(thsum, arg_f2(cb.det.re.hi, cb.det.im.hi, cb.det.re.lo, cb.det.im.lo)), edge);
+    const float apsi = apsi2.hi + apsi2.lo;
     FT_DBG(26, apsi);
-    FT_DBG(27, growth);
-    FT_DBG(28, mag / vabs);
-    FT_DBG(29, jgrowth);
-    FT_DBG(30, thsum.hi);
-    FT_DBG(31, (float)(cpsi.e - psi.e) + log2f(cpsi.m / psi.m));
-    if (edge || cpsi.bad || mv.bad || mj.bad || !(jgrowth > PIVOT_GROWTH)) {
+    if (edge) {
         need64 = true;
         return false;
     }
-    // log2|cR / IGtr| and arg cR
-    const f2 lpsi = log2_ratio(cpsi, lFs);
-    const f2 lv = log2_ratio(mv, lGs);
+    // log2 |cPsi| and log2 |V| (exponents exact, small parts in FP32), then
+    // log2 |cR / IGtr| = -D/2 log2(|cPsi| / psi_tr) - W log2(|V| / V_tr) + log2 |det J|
+    const float l2dm = 0.5f * m_log2(dn2), l2vm = 0.5f * m_log2(vn2);
+    const f2 l2psi_abs = f2_add(f2_add(f2_mul2(sumlx, f2_make(RLN2_HI, RLN2_LO)), (float)cb.det_e), l2dm);
+    const f2 lpsi = f2_add2(l2psi_abs, f2_neg(f2_mul2(lFs, f2_make(RLN2_HI, RLN2_LO))));
+    const f2 l2v_abs = f2_add(f2_make((float)v_e, 0.0f), l2vm);
+    const f2 lv = f2_add2(l2v_abs, f2_neg(f2_mul2(lGs, f2_make(RLN2_HI, RLN2_LO))));
     f2 t = f2_add2(f2_mulf(lpsi, -D2), f2_mulf(lv, -W));
-    t = f2_add(t, (float)mj.e);
-    t = f2_add(t, m_log2(mj.m));
+    t = f2_add(t, (float)pj_e);
+    t = f2_add(t, 0.5f * m_log2(fmaf(pj.re, pj.re, pj.im * pj.im)));
     // arg cR = -D/2 arg cPsi + arg det J + nu . theta - W arg V (two-float sum)
     f2 angf = f2_add2(f2_mulf(apsi2, -D2), xnu);
-    angf = f2_add(angf, m_atan2(pj.im, pj.re));
-    angf = f2_add(angf, -W * av);
+    angf = f2_add2(angf, arg_f2(pj.re, pj.im, 0.0f, 0.0f));
+    angf = f2_add2(angf, f2_mulf(av2, -W));
     const float ang = angf.hi;
     const float mod = m_exp2(t.hi) * (1.0f + t.lo * LN2_F);
     float sn, cs;
@@ -1858,8 +1875,9 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     cx<float> c = cmk(IGtr * mod * cs, IGtr * mod * sn);
     out[0] = c;
     if (FT_K > 1) {
-        const float er =
-            LN2_F * ((float)(cpsi.e - FT_LOOPS * mv.e) + (m_log2(cpsi.m) - (float)FT_LOOPS * m_log2(mv.m)));
+        // log cPsi - L log V (srcs/feynman_integral.hpp:336-341): the large parts in two-float
+        const f2 dl = f2_add2(l2psi_abs, f2_mulf(l2v_abs, -(float)FT_LOOPS));
+        const float er = LN2_F * (dl.hi + dl.lo);
         const float ei = apsi - (float)FT_LOOPS * av;
 #pragma unroll
         for (int j = 1; j < FT_K; j++) {
@@ -2068,7 +2086,7 @@ struct accum {
     int since_fold;
     float keptf, droppedf, queuedf, exactf;   // counters below 2^24 between folds
 #endif
-    double kept, dropped, queued, exact, robust, vpass;
+    double kept, dropped, queued, exact, robust;
 
     __device__ __forceinline__ void init(unsigned char* smem_acc)
     {
@@ -2090,7 +2108,7 @@ struct accum {
             Cf[s * FT_BLOCK] = 0.0f;
 #endif
         }
-        kept = dropped = queued = exact = robust = vpass = 0.0;
+        kept = dropped = queued = exact = robust = 0.0;
     }
 
     __device__ __forceinline__ void nadd(int slot, double v)
@@ -2185,7 +2203,6 @@ struct accum {
         vals[ACC_ROBUST] = robust;
 #pragma unroll
         for (int s = ACC_ROBUST + 1; s < ACC_SLOTS; s++) vals[s] = 0.0;
-        vals[ACC_VPASS] = vpass;
         block_reduce(vals, dst);
     }
 };
@@ -2234,30 +2251,6 @@ static __device__ __forceinline__ void sample64(xo& g, const table_ref& tr, cons
 }
 #endif
 
-#if FT_VPASS
-// the V pass buffer after the per-thread sums: 2 FT_BLOCK entries of 5 words (the
-// sample as in the FP64 queue, and its stream state), then the entry count
-#define VBUF_OFFSET ((ACC_SMEM_OFFSET + FT_BLOCK * ACC_BYTES_PER_THREAD + 15u) & ~15u)
-// one sample of the V pass from its stream state: the sector redrawn, the integrand
-// with V in two-float; 0 kept, 1 dropped, 2 for the FP64 pass
-static __device__ __noinline__ int vpass_eval(u64 sa, u64 sb, u64 sc, u64 sd, const table_ref* tr, const float* pf,
-                                             const float* pd, cx<float>* R, unsigned char* ord)
-{
-    xo g;
-    g.a = sa;
-    g.b = sb;
-    g.c = sc;
-    g.d = sd;
-    f2 lx[FT_E], lF, lG;
-    draw_sector32(g, *tr, pf, lx, lF, lG, ord);
-#pragma unroll
-    for (int j = 0; j < FT_K; j++) R[j] = cmk(0.0f, 0.0f);
-    bool need64 = false, vfail = false;
-    const bool ok = integrand32<true>(pd, pf, lx, lF, lG, R, need64, vfail);
-    return need64 ? 2 : (ok ? 0 : 1);
-}
-#endif
-
 // ------------------------------------------------------------------ one thread's samples
 // Samples [first, last) of the stream, g holding the state of sample `first`.  In the
 // mixed form, samples whose FP32 evaluation is not trustworthy are queued for the FP64
@@ -2276,58 +2269,12 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
 #endif
     (void)qtag;
     (void)chunk;
-#if FT_VPASS
-    extern __shared__ __align__(16) unsigned char smem[];
-    u64* vbuf = (u64*)(smem + VBUF_OFFSET);
-    unsigned int* vcnt = (unsigned int*)(vbuf + 2 * FT_BLOCK * 5);
-    if (threadIdx.x == 0) *vcnt = 0u;
-    // entries [n - m, n) of the buffer, one per thread
-    auto vflush = [&](unsigned int n, unsigned int m) {
-        if (threadIdx.x < m) {
-            const u64* v = vbuf + (size_t)(n - m + threadIdx.x) * 5;
-            cx<float> Rv[FT_K];
-            unsigned char ordv[FT_E];
-            const int st = vpass_eval(v[1], v[2], v[3], v[4], &tr, pf, pd, Rv, ordv);
-            unsigned char fl = REC_VPASS;
-            A.vpass += 1.0;
-            if (st == 2) {
-                fl |= REC_QUEUED;
-                A.note32(0.0f, 1.0f, 0.0f);
-                const unsigned int slot = atomicAdd(qcount, 1u);
-                if (slot < qcap) {
-                    u64* q = queue + (size_t)slot * 5;
-#pragma unroll
-                    for (int w = 0; w < 5; w++) q[w] = v[w];
-                }
-            } else if (st == 1) {
-                fl |= REC_DROPPED;
-                A.note32(1.0f, 0.0f, 0.0f);
-            } else {
-                A.add32(Rv);
-            }
-#if !FT_BATCH
-            if (FT_RECORD) write_record(v[0], ordv, Rv, st == 0, fl, rec_order, rec_R, rec_flags);
-#endif
-        }
-    };
-#endif
 #if FT_VARIANT & 4
     // Every thread of the block makes `chunk` trips and the block starts each sample
     // together: the warps then run the same stretch of the (long, straight-line)
     // per-sample code at the same time and share its instruction fetches.
     for (u64 k = 0; k < chunk; k++) {
         __syncthreads();
-#if FT_VPASS
-        {
-            const unsigned int n = *vcnt;   // the same for the whole block (read after the barrier)
-            if (n >= FT_BLOCK) {
-                vflush(n, FT_BLOCK);
-                __syncthreads();
-                if (threadIdx.x == 0) *vcnt = n - FT_BLOCK;
-                __syncthreads();
-            }
-        }
-#endif
         const u64 i = first + k;
         if (i >= last) continue;
 #else
@@ -2347,29 +2294,8 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
         if (ex) flags |= REC_EXACT;
         if (FT_RECORD)
             for (int e = 0; e < FT_E; e++) rec_X[i * FT_E + e] = exp((double)lx[e].hi + (double)lx[e].lo);
-        bool need64 = false, vfail = false;
-        const bool ok = integrand32<false>(pd, pf, lx, lF, lG, R, need64, vfail);
-        (void)vfail;
-#if FT_VPASS
-        if (need64 && vfail) {
-            // fewer than FT_BLOCK entries before this sample: the slot stays in the buffer
-            const unsigned int s2 = atomicAdd(vcnt, 1u);
-            u64* v = vbuf + (size_t)s2 * 5;
-#if FT_BATCH
-            v[0] = qtag | (i - first);
-#else
-            v[0] = i;
-#endif
-            v[1] = g0.a;
-            v[2] = g0.b;
-            v[3] = g0.c;
-            v[4] = g0.d;
-            A.note32(0.0f, 0.0f, (float)ex);
-            if (FT_RECORD)
-                write_record(i, ord, R, false, (unsigned char)(flags | REC_VPASS), rec_order, rec_R, rec_flags);
-            continue;
-        }
-#endif
+        bool need64 = false;
+        const bool ok = integrand32(pd, pf, lx, lF, lG, R, need64);
         if (need64) {
             flags |= REC_QUEUED;
             A.note32(0.0f, 1.0f, (float)ex);
@@ -2399,19 +2325,6 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
         if (FT_RECORD) write_record(i, ord, R, ok, flags, rec_order, rec_R, rec_flags);
 #endif
     }
-#if FT_VPASS
-    // the rest of the buffer, in rounds of at most FT_BLOCK entries
-    __syncthreads();
-    {
-        unsigned int n = *vcnt;
-        while (n > 0) {
-            const unsigned int m = n < FT_BLOCK ? n : FT_BLOCK;
-            vflush(n, m);
-            n -= m;
-        }
-    }
-    __syncthreads();
-#endif
 }
 
 #if !FT_BATCH
@@ -2560,14 +2473,41 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample_batch(
 }
 
 #if FT_PREC == 0
+// Exact, order-independent sum of doubles: digit j of an accumulator (a signed 64-bit
+// counter) weighs 2^(32 j - 1074); v = m 2^(p - 1074) with its integer significand m
+// (53 bits) enters as the three 32-bit digits of m 2^(p mod 32) at digit p / 32, so
+// every add is exact and integer addition makes the result independent of the order
+// in which the threads' atomics land.  Non-finite values are not added (the FP64 pass
+// keeps only finite samples).
+static __device__ __forceinline__ void exact_add(u64* __restrict__ dig, double v)
+{
+    const u64 b = (u64)__double_as_longlong(v);
+    const int be = (int)((b >> 52) & 0x7ffull);
+    if (be == 0x7ff) return;
+    u64 m = b & 0xfffffffffffffull;
+    int p = 0;
+    if (be) {
+        m |= 1ull << 52;
+        p = be - 1;
+    }
+    if (m == 0) return;
+    const int j = p >> 5, sh = p & 31;
+    const u64 lo = m << sh, hi = sh ? (m >> (64 - sh)) : 0ull;
+    const bool neg = (b >> 63) != 0;
+    const u64 c0 = lo & 0xffffffffull, c1 = lo >> 32;
+    atomicAdd(dig + j, neg ? 0ull - c0 : c0);
+    if (c1) atomicAdd(dig + j + 1, neg ? 0ull - c1 : c1);
+    if (hi) atomicAdd(dig + j + 2, neg ? 0ull - hi : hi);
+}
+
 // FP64 pass over the samples a mixed batch launch queued: each entry names its work
-// item (hence the instance) and carries the sample's stream state.  Sums go to the
-// instance's slots of qacc with atomics: per eps order j [4j + 0..3] = re f, re f^2,
-// im f, im f^2, then [4K] kept, [4K+1] dropped, [4K+2] robust.
-#define QACC_SLOTS (4 * FT_K + 4)
+// item (hence the instance) and carries the sample's stream state.  Each kept sample's
+// values go exactly into the instance's accumulators in qacc (FT_XA_DIGITS words each):
+// per eps order j accumulators 4j + 0..3 = re f, re f^2, im f, im f^2; then the
+// counters kept, dropped, robust (integer atomics).
 extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue_batch(
     const batch_inst* __restrict__ inst, int ninst, const u64* __restrict__ queue,
-    const unsigned int* __restrict__ qcount, unsigned int qcap, double* __restrict__ qacc)
+    const unsigned int* __restrict__ qcount, unsigned int qcap, u64* __restrict__ qacc)
 {
     unsigned int n = *qcount;
     if (n > qcap) n = qcap;
@@ -2597,21 +2537,22 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK) ft_sample_queue_batch(
         draw_sector64(g, tr, prm[P_JRFULL], X, F, Gv, ord);
         bool rob = false;
         const bool ok = integrand64(prm, X, F, Gv * F, R, rob);
-        double* qa = qacc + (size_t)id * QACC_SLOTS;
-        if (rob) atomicAdd(qa + 4 * FT_K + 2, 1.0);
+        u64* qa = qacc + (size_t)id * (4 * FT_K * FT_XA_DIGITS + 4);
+        u64* cnt = qa + 4 * FT_K * FT_XA_DIGITS;
+        if (rob) atomicAdd(cnt + 2, 1ull);
         if (!ok) {
-            atomicAdd(qa + 4 * FT_K + 1, 1.0);
+            atomicAdd(cnt + 1, 1ull);
             continue;
         }
-        atomicAdd(qa + 4 * FT_K, 1.0);
+        atomicAdd(cnt, 1ull);
 #pragma unroll
         for (int j = 0; j < FT_K; j++) {
             if (FT_ONLY_PSI && j > 0) break;
-            atomicAdd(qa + 4 * j + 0, R[j].re);
-            atomicAdd(qa + 4 * j + 1, R[j].re * R[j].re);
+            exact_add(qa + (4 * j + 0) * FT_XA_DIGITS, R[j].re);
+            exact_add(qa + (4 * j + 1) * FT_XA_DIGITS, R[j].re * R[j].re);
             if (ACC_PARTS == 4) {
-                atomicAdd(qa + 4 * j + 2, R[j].im);
-                atomicAdd(qa + 4 * j + 3, R[j].im * R[j].im);
+                exact_add(qa + (4 * j + 2) * FT_XA_DIGITS, R[j].im);
+                exact_add(qa + (4 * j + 3) * FT_XA_DIGITS, R[j].im * R[j].im);
             }
         }
     }

@@ -53,6 +53,12 @@ void fill_result(const ft::prepared& P, const std::vector<double>& acc, ft_resul
 
 struct ft_plan {
     ft::prepared P;
+    // the kernels' vertex labels: vertices without external momentum first, the external
+    // ones last, the last of them the deleted (ground) vertex; kek/kel the edges in these
+    // labels and kP the scalar products; reduced vertices [0, q0) carry no momentum
+    std::vector<int> kek, kel;
+    std::vector<double> kP;
+    int q0 = 0;
     std::vector<double> sigma, q, prm;
     std::vector<unsigned char> tab;
     int device = 0;
@@ -99,8 +105,9 @@ struct ft_plan {
         k.mode = P.deformed() ? 1 : 0;
         k.only_psi = P.only_psi() ? 1 : 0;
         k.record = record;
-        k.ek = P.ek;
-        k.el = P.el;
+        k.ek = kek;
+        k.el = kel;
+        k.q0 = q0;
         // small tables are staged per block in shared memory; from E = 11 on the table is
         // read through L1 (one cached copy per SM instead of one per block)
         k.table_global = P.E >= 11 ? 1 : 0;

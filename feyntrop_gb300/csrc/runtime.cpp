@@ -109,14 +109,45 @@ using namespace ftrt;
 
 namespace {
 
-// P~ = P restricted to vertices 0..V-2 (vertex V-1 is the deleted one), split as
-// sum_r sigma_r q_r q_r^T; eigenpairs with |sigma| <= 1e-14 max|sigma| are dropped
-void low_rank(const ft::prepared& p, std::vector<double>& sigma, std::vector<double>& q)
+// The kernels' vertex labels (any labelling gives the same integrand; the reference
+// deletes a vertex chosen per sample, srcs/feynman_integral.hpp:166-194): vertices whose
+// row of P is zero first, in their order, then the external ones, the last external
+// vertex being the deleted one.  The eliminations then remove the internal vertices
+// first, and the quadratic forms of P~ only involve the external rows [q0, V-1).
+void relabel(ft_plan& pl)
 {
-    const int n = p.V - 1;
+    const ft::prepared& p = pl.P;
+    const int V = p.V;
+    std::vector<int> ext(V, 0), lab(V, -1);
+    for (int v = 0; v < V; v++)
+        for (int w = 0; w < V; w++) ext[v] |= p.P[(size_t)v * V + w] != 0.0;
+    int next = 0;
+    for (int pass = 0; pass < 2; pass++)
+        for (int v = 0; v < V; v++)
+            if (ext[v] == pass) lab[v] = next++;
+    int nint = 0;
+    for (int v = 0; v < V; v++) nint += !ext[v];
+    pl.q0 = nint == V ? V - 1 : nint;
+    pl.kek.resize(p.E);
+    pl.kel.resize(p.E);
+    for (int e = 0; e < p.E; e++) {
+        const int a = lab[p.ek[e]], b = lab[p.el[e]];
+        pl.kek[e] = a > b ? a : b;
+        pl.kel[e] = a > b ? b : a;
+    }
+    pl.kP.assign((size_t)V * V, 0.0);
+    for (int v = 0; v < V; v++)
+        for (int w = 0; w < V; w++) pl.kP[(size_t)lab[v] * V + lab[w]] = p.P[(size_t)v * V + w];
+}
+
+// P~ = kP restricted to vertices 0..V-2 (vertex V-1 is the deleted one), split as
+// sum_r sigma_r q_r q_r^T; eigenpairs with |sigma| <= 1e-14 max|sigma| are dropped
+void low_rank(const std::vector<double>& P, int V, std::vector<double>& sigma, std::vector<double>& q)
+{
+    const int n = V - 1;
     std::vector<double> A((size_t)n * n), Vv((size_t)n * n, 0.0);
     for (int i = 0; i < n; i++)
-        for (int j = 0; j < n; j++) A[i * n + j] = p.P[i * p.V + j];
+        for (int j = 0; j < n; j++) A[i * n + j] = P[i * V + j];
     for (int i = 0; i < n; i++) Vv[i * n + i] = 1.0;
     for (int sweep = 0; sweep < 100; sweep++) {
         double off = 0;
@@ -293,19 +324,21 @@ struct launch_geometry {
 // drift apart and the block waits at its final reduction for its slowest warp (the
 // 5-loop cube ran 6x slower at 2570 samples per thread than at 128).  Kernels with the
 // barrier keep their warps together and run one wave of long chunks (more waves cost
-// them 1-2 % per halving of the chunk).  waves = false: one wave (the no-allocation
-// path, whose scratch holds a bounded number of blocks).
-launch_geometry geometry(const ft::kernel_set& ks, unsigned long long N, bool waves = true)
+// them 1-2 % per halving of the chunk).  max_blocks bounds the waves (the
+// no-allocation path, whose scratch holds a bounded number of blocks).
+launch_geometry geometry(const ft::kernel_set& ks, unsigned long long N, unsigned long long max_blocks = ~0ull)
 {
-    const unsigned long long per_wave = (unsigned long long)dev_state().sms * ks.blocks_per_sm * ks.block;
+    const unsigned long long wave_blocks = (unsigned long long)dev_state().sms * ks.blocks_per_sm;
+    const unsigned long long per_wave = wave_blocks * ks.block;
     unsigned long long w = 1;
-    if (waves && N > 0 && !(ks.variant & 4)) {
+    if (N > 0 && !(ks.variant & 4)) {
         static const unsigned long long cap = [] {
             const char* e = std::getenv("FEYNTROP_GB300_CHUNK_CAP");
             const unsigned long long v = e ? std::strtoull(e, nullptr, 10) : 128ull;
             return v ? v : 128ull;
         }();
         w = std::max(1ull, (N + per_wave * cap - 1) / (per_wave * cap));
+        w = std::min(w, std::max(1ull, max_blocks / wave_blocks));
     }
     const unsigned long long max_threads = per_wave * w;
     launch_geometry g;
@@ -504,7 +537,8 @@ static std::unique_ptr<ft_plan> make_plan(const ft_problem* pb, int threads, int
     std::unique_ptr<ft_plan> pl(new ft_plan());
     pl->P = ft::prepare(in, threads);
     if (pl->P.E > 24) throw std::domain_error("graphs with more than 24 edges are not supported by the GPU sampler");
-    low_rank(pl->P, pl->sigma, pl->q);
+    relabel(*pl);
+    low_rank(pl->kP, pl->P.V, pl->sigma, pl->q);
     build_blocks(*pl);
     pl->device = device;
     return pl;
@@ -630,7 +664,8 @@ int ft_precompile(const ft_problem* pb, int32_t precision, double* seconds)
         ft::problem_input in = input_of(pb);
         ft_plan pl;
         pl.P = ft::prepare(in);
-        low_rank(pl.P, pl.sigma, pl.q);
+        relabel(pl);
+        low_rank(pl.kP, pl.P.V, pl.sigma, pl.q);
         auto t0 = std::chrono::steady_clock::now();
         const int prec = precision & 0xff;
         const bool batch = (precision & FT_PRECOMPILE_BATCH) != 0;
@@ -735,8 +770,10 @@ int ft_integrate_noalloc(ft_plan* pl, const ft_run_options* o, double* d_slots)
                 "precision first (loading them allocates)");
         const unsigned long long N = o->num_samples;
         if (N == 0) throw std::invalid_argument("ft_integrate_noalloc: num_samples must be positive");
-        const launch_geometry g = geometry(*ks, N, false);
         const unsigned qblocks = prec ? (unsigned)(dev_state().sms * std::max(1, k64->queue_blocks_per_sm)) : 0;
+        // ft_integrate's launch shape, its waves capped to the blocks the scratch holds
+        const launch_geometry g =
+            geometry(*ks, N, qblocks < NOALLOC_MAX_BLOCKS ? (unsigned long long)(NOALLOC_MAX_BLOCKS - qblocks) : 1ull);
         if (g.blocks + qblocks > NOALLOC_MAX_BLOCKS || g.lanebits > NOALLOC_MAX_LANE_BITS)
             throw std::invalid_argument("ft_integrate_noalloc: launch exceeds the static scratch (2048 blocks)");
         ft::noalloc_layout sc;
@@ -804,16 +841,18 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
             s.variant = variant;
             cands.push_back(s);
         };
-        if (prec == 1) {
-            const int v = deformed ? 1 : 0;
-            for (int var : {v | 4, v})
-                for (int bm : {512, 256, 128}) add(bm, 512 / bm, var);
-            if (deformed) {
-                add(512, 1, 4);
-                // the V pass (bit 3): pays where many samples fail only for V's rounding
-                add(256, 2, 13);
-                add(512, 1, 13);
+        if (prec == 1 && deformed) {
+            // two-float determinant and V: out-of-line routines (bit 3) and shapes from 128
+            // registers (16 warps per SM) to 255 (8 warps, no spills)
+            for (int var : {13, 5}) {
+                add(512, 1, var);
+                add(256, 2, var);
+                add(256, 1, var);
             }
+            add(384, 1, 13);
+        } else if (prec == 1) {
+            for (int var : {4, 0})
+                for (int bm : {512, 256, 128}) add(bm, 512 / bm, var);
         } else {
             const int v = deformed ? 1 : 0;
             for (int var : {v | 4, v})

@@ -154,14 +154,17 @@ int ft_batch_get_info(const ft_batch* batch, ft_batch_info* info);
 /* Integration that allocates no memory, for callers that must not allocate device
  * memory while they integrate (an embedding application or serving loop that owns all
  * device memory, or a region where allocation is forbidden).  No counterpart in the
- * reference.  Same samples and the same launches as ft_integrate, asynchronous on
- * opts->stream (or the plan's stream): the final sums are written to d_slots, a
- * caller-owned DEVICE buffer of 8K+8 doubles: for eps order j and part p (0 Re, 1 Im)
- * [8j+4p .. +3] = sum f (hi, lo), sum f^2 (hi, lo); then kept, dropped, FP64
- * re-evaluated, exact sector steps, complete-pivoting factorisations.
+ * reference.  The same samples as ft_integrate, and its launch shape with the number
+ * of blocks capped at what the scratch holds, asynchronous on opts->stream (or the
+ * plan's stream): the final sums are written to d_slots, a caller-owned DEVICE buffer
+ * of 8K+8 doubles: for eps order j and part p (0 Re, 1 Im) [8j+4p .. +3] = sum f
+ * (hi, lo), sum f^2 (hi, lo); then kept, dropped, samples handed to the FP64 pass
+ * (all of them, also those beyond the queue), exact sector steps, complete-pivoting
+ * factorisations.
  * Scratch is one static device array per GPU (about 7 MB, held until exit): at most
- * 2048 blocks, 16 eps orders and 65536 samples handed to the FP64 pass per call (more
- * are not evaluated: kept + dropped < N reports it).  The plan's kernels must already be
+ * 2048 blocks, 16 eps orders and 65536 samples handed to the FP64 pass per call; the
+ * hand-offs beyond 65536 are not evaluated, which slot 8K+2 > 65536 (equivalently
+ * kept + dropped < N) reports.  The plan's kernels must already be
  * loaded by one ft_integrate call with the same precision.  The first call on a device
  * looks up the scratch address (call it once before any stream capture).  Calls share
  * the scratch, so calls that overlap on the GPU race. */

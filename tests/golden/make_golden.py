@@ -181,6 +181,18 @@ def extra_cases():
                         "masses_sqr": [rng.uniform(0, 3) for _ in range(10)], "num_eps_terms": 3, "lambda": 0,
                         "N": 1000, "seed": 0}
 
+    # the same ladder at a Minkowski point (the deformed class of the mixed batch):
+    # on-shell externals p_i^2 = 1, s U[8, 20], t U[-6, -1], masses U[0, 3] from
+    # Random(7), lambda = 0.5, through the reference's front end
+    rng = random.Random(7)
+    m2 = [rng.uniform(0, 3) for _ in range(10)]
+    s, t = rng.uniform(8, 20), rng.uniform(-6, -1)
+    c["ladder3_4pt_mink"] = kin_input(
+        [(tuple(e), nu, "m%d" % i) for i, (e, nu) in enumerate(ladder)],
+        [(sp[0, 0], "1"), (sp[1, 1], "1"), (sp[2, 2], "1"), (sp[0, 1], "(S-2)/2"), (sp[1, 2], "(T-2)/2"),
+         (sp[0, 2], "(2-S-T)/2")],
+        [("m%d" % i, m2[i]) for i in range(10)] + [("S", s), ("T", t)], 4, 3, 0.5)
+
     # 4-loop wheel vacuum graph, all masses 1, P = 0
     wheel = [[[0, 1], 1], [[1, 2], 1], [[2, 3], 1], [[3, 0], 1], [[0, 4], 1], [[1, 4], 1], [[2, 4], 1],
              [[3, 4], 1]]
@@ -233,10 +245,16 @@ def run_harness(inp, args):
 
 
 def main():
+    """All cases, or with `--only name ...` just those, merged into the existing pins."""
     cases = suite_cases()
     cases.update(extra_cases())
     pins = {"generator": "tests/golden/make_golden.py", "N_aggregate": N_AGG, "seeds": SEEDS, "cases": {},
             "suite_expectations": suite_expectations(), "suite_symbolic": SYMBOLIC}
+    if "--only" in sys.argv:
+        only = sys.argv[sys.argv.index("--only") + 1:]
+        with open(os.path.join(HERE, "reference_pins.json")) as f:
+            pins = json.load(f)
+        cases = {k: v for k, v in cases.items() if k in only}
     for name, inp in cases.items():
         print("case", name, flush=True)
         table = run_harness(inp, ["table"])

@@ -21,7 +21,7 @@ pytestmark = pytest.mark.gpu
 
 PINS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_pins.json")))
 NAMES = ["C1_K4", "C2_double_box", "2L_5pt_box_pent", "C3_box_pentagon_0", "1L_3pt_eucl", "2L_3pt_tutorial",
-         "wheel4_vacuum"]
+         "wheel4_vacuum", "ladder3_4pt_mink"]
 TOL = {ft.FP64: 1e-6, ft.MIXED: 1e-3}
 
 
@@ -48,8 +48,8 @@ def plans():
 
 @pytest.mark.parametrize("precision", [ft.FP64, ft.MIXED])
 def test_batch_equals_single_integrals(plans, precision):
-    Ns = [1_500_000, 700_001, 1_000_003, 333_333, 2_000_000, 123_457, 999_999]
-    seeds = [0, 1, 2, 3, 4, 5, 6]
+    Ns = [1_500_000, 700_001, 1_000_003, 333_333, 2_000_000, 123_457, 999_999, 800_001]
+    seeds = [0, 1, 2, 3, 4, 5, 6, 7]
     b = ft.Batch(plans, precision)
     out = b.run(Ns, seeds)
     info = b.info()
@@ -65,7 +65,7 @@ def test_batch_is_reusable_with_new_seeds_and_offsets(plans):
     b = ft.Batch(plans, ft.MIXED)
     b.run(200_000, seeds=1)
     captures = b.info()["graph_captures"]
-    out = b.run(150_000, seeds=9, first_samples=[0, 10, 20, 30, 40, 50, 60])
+    out = b.run(150_000, seeds=9, first_samples=[0, 10, 20, 30, 40, 50, 60, 70])
     assert b.info()["graph_captures"] == captures   # fewer items than before: graph replayed
     for i, p in enumerate(plans):
         r = p.integrate(150_000, seed=9, precision=ft.MIXED, first_sample=10 * i)
@@ -95,6 +95,54 @@ def test_integrate_batch_splits_precisions(plans):
         b = ras[i].as_dict(p.info["IGtr"])
         r = p.integrate(N[i], seed=3, precision=precs[i])
         assert_same(b, r, precs[i], NAMES[i])
+
+
+def test_sharded_batch_blocks_merge_to_one_run(plans):
+    """The GPU side of a sharded batch (feyntrop_gb300.shard.batch_sharded, mode
+    "samples"): the two ranks' sample blocks of every integral, run as batches and
+    merged, equal one run of the whole batch (the same samples; sums to rounding)."""
+    from feyntrop_gb300 import shard
+    b = ft.Batch(plans, ft.FP64)
+    Ns = [300_001, 200_000, 250_003, 100_000, 400_000, 50_001, 300_000, 120_001]
+    full = b.run(Ns, seeds=5)
+    blocks = []
+    for r in range(2):
+        fc = [shard.split_samples(N, r, 2) for N in Ns]
+        blocks.append(b.run([c for _, c in fc], seeds=5, first_samples=[f for f, _ in fc]))
+    for i, p in enumerate(plans):
+        m = shard.merge_moments([blocks[0][i]["moments"], blocks[1][i]["moments"]])
+        assert [x[0] for x in m] == [x[0] for x in full[i]["moments"]], NAMES[i]
+        merged = ft.finalize_moments(m, p.K, real_only=not p.info["deformed"])
+        for j, ((re, dre), (im, dim)) in enumerate(full[i]["integral"]):
+            (mre, mdre), (mim, mdim) = merged[j]
+            assert abs(mre - re) <= 1e-6 * dre and abs(mdre - dre) <= 1e-6 * dre, (NAMES[i], j)
+            assert abs(mim - im) <= 1e-6 * max(dim, 1e-300) or (dim == 0 and mim == 0), (NAMES[i], j)
+    b.close()
+
+
+def test_batch_runs_are_bit_identical():
+    """The FP64 pass of a mixed batch adds its samples into exact fixed-point
+    accumulators, so the order in which the queue's entries are handled does not
+    matter: the same batch run twice gives bit-identical sums.  The double box at its
+    Minkowski point without the deformation (lambda = 0, one eps order; the reference
+    accepts it) has V changing sign inside the domain, and the FP32 evaluation hands
+    every sample with V near or below zero to the FP64 pass; deformed integrals beside it."""
+    undeformed = dict(workloads.double_box(N=1000, lam=0.0), num_eps_terms=1)
+    names = ["double box, lambda 0", "2L_3pt_tutorial", "C3_box_pentagon_1", "1L_3pt_mink"]
+    ps = [ft.Plan(undeformed)] + [ft.Plan(PINS["cases"][n]["input"]) for n in names[1:]]
+    assert not ps[0].info["deformed"]
+    b = ft.Batch(ps, ft.MIXED)
+    Ns = [2_000_000, 2_000_000, 1_000_000, 500_000]
+    first = b.run(Ns, seeds=[1, 2, 3, 4])
+    second = b.run(Ns, seeds=[1, 2, 3, 4])
+    assert first[0]["fp64_fallback"] > 10_000
+    for a, c, n in zip(first, second, names):
+        assert a["kept"] == c["kept"] and a["dropped"] == c["dropped"], n
+        assert a["moments"] == c["moments"], n
+        assert a["integral"] == c["integral"], n
+    b.close()
+    for p in ps:
+        p.close()
 
 
 def test_kinematic_scan_batch():
@@ -162,7 +210,7 @@ def test_autotune_records_a_shape_and_keeps_the_samples():
     before = p.integrate(300_000, seed=8, precision=ft.MIXED)
     t = p.autotune(ft.MIXED, samples=1_000_000)
     assert t["candidates"] >= 4 and t["samples_per_second"] > 0
-    assert t["block"] in (64, 128, 256, 512) and t["variant"] in range(16)
+    assert t["block"] in (64, 128, 256, 384, 512) and t["variant"] in range(16)
     assert t["samples_per_second"] >= t["default_samples_per_second"]
     assert t["batch_chunk"] in (32, 64, 128, 256) and t["batch_samples_per_second"] > 0
     after = p.integrate(300_000, seed=8, precision=ft.MIXED)

@@ -84,6 +84,72 @@ def test_two_gloo_ranks_equal_one_run_over_all_samples(name):
             assert abs(dim - ref[j, 3]) <= 1e-8 * ref[j, 3]
 
 
+BATCH = ["C1_K4", "1L_3pt_mink", "1L_3pt_eucl"]   # three integrals, two topologies
+BATCH_N = [15001, 12000, 9999]
+
+
+def _batch_rank_main(rank, world, port, mode, result_path):
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        import feyntrop_gb300 as ft
+        from feyntrop_gb300 import shard
+        inputs = [PINS["cases"][n]["input"] for n in BATCH]
+        Ks = [x["num_eps_terms"] for x in inputs]
+        real_only = [not ft.subgraph_table(x)[4]["deformed"] for x in inputs]
+
+        def run(mine, seeds, firsts):
+            # this rank's part of the batch, from the oracle's per-sample values
+            return [None if N is None else {"moments": shard_moments(x, s, f, N)}
+                    for x, N, s, f in zip(inputs, mine, seeds, firsts)]
+
+        integrals, _ = shard.batch_sharded(run, BATCH_N, Ks, real_only, rank, world, seeds=[3, 4, 5], mode=mode)
+        if rank == 0:
+            with open(result_path, "w") as f:
+                json.dump(integrals, f)
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+@pytest.mark.parametrize("mode", ["samples", "integrals"])
+def test_sharded_batch_equals_one_run(mode):
+    """A 3-integral, 2-topology batch over two gloo ranks (each rank its block of every
+    integral's samples, or its share of the integrals), merged, against one run of every
+    integral over all its samples."""
+    mp = pytest.importorskip("torch.multiprocessing")
+    import oracle_lib as ol
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "merged.json")
+        mp.start_processes(_batch_rank_main, args=(2, free_port(), mode, path), nprocs=2, start_method="spawn")
+        merged = json.load(open(path))
+    for name, N, seed, got in zip(BATCH, BATCH_N, [3, 4, 5], merged):
+        inp = PINS["cases"][name]["input"]
+        ref, _, _ = ol.Prepared(inp).integrate(N, seed, 1)
+        for j in range(inp["num_eps_terms"]):
+            (re, dre), (im, dim) = got[j]
+            assert abs(re - ref[j, 0]) <= 1e-12 * abs(ref[j, 0]) + 1e-15, (name, j, re, ref[j])
+            assert abs(dre - ref[j, 1]) <= 1e-8 * ref[j, 1], (name, j, dre, ref[j])
+            if ref[j, 3] == 0:
+                assert im == 0 and dim == 0
+            else:
+                assert abs(im - ref[j, 2]) <= 1e-12 * abs(ref[j, 2]) + 1e-15
+
+
+def test_split_samples_covers_the_range():
+    from feyntrop_gb300 import shard
+    for N in (0, 1, 7, 1000, 12345):
+        for world in (1, 2, 3, 8):
+            parts = [shard.split_samples(N, r, world) for r in range(world)]
+            assert sum(c for _, c in parts) == N
+            pos = 0
+            for f, c in parts:
+                assert f == pos
+                pos += c
+
+
 def test_merge_rejects_mismatched_shards():
     from feyntrop_gb300 import shard
     with pytest.raises(ValueError):
