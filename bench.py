@@ -108,6 +108,31 @@ def dram_traffic(key):
     return None
 
 
+def instructions_per_sample(key):
+    """Thread instructions executed per sample by a kernel, from the committed ncu
+    summary profiles/instructions.txt (lines: kernel, precision, workload, count)."""
+    path = os.path.join(HERE, "profiles", "instructions.txt")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        parts = line.split()
+        if len(parts) >= 4 and not line.startswith("#") and " ".join(parts[:3]) == key:
+            return float(parts[3])
+    return None
+
+
+def issue_roofline(key, samples_per_s, sm_mhz, sms):
+    """Executed thread instructions per second (counted per sample by ncu, times the
+    live rate) against the issue capacity: SMs x 4 schedulers x 32 lanes x clock."""
+    ips = instructions_per_sample(key)
+    if ips is None or not sm_mhz:
+        return None
+    peak = sms * 4 * 32 * sm_mhz * 1e6 / 1e12
+    ach = samples_per_s * ips / 1e12
+    return {"achieved": ach, "peak": peak, "unit": "T thread-instructions/s", "frac": ach / peak,
+            "instructions_per_sample": ips, "source": "profiles/instructions.txt (ncu, %s)" % key}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
 
@@ -656,6 +681,9 @@ def main():
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": traffic,
                      "hbm": hbm,
+                     "issue": issue_roofline("ft_sample mixed double_box", N / (kms * 1e-3),
+                                             clocks.get("sm_mhz"),
+                                             torch.cuda.get_device_properties(local).multi_processor_count),
                      "flops_per_sample": flops,
                      "note": "algorithmic flops per sample %.0f of the reference's loop, %s: the oracle's "
                              "restatement run with an operation-counting scalar (profiles/flop_counts.txt) x samples "

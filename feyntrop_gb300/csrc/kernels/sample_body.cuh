@@ -66,7 +66,8 @@ typedef unsigned int u32;
 // SM streams per sample fits the instruction caches better; bit 2 starts every sample
 // with a block-wide barrier, so that the block's warps walk the code together and
 // share its instruction fetches; bit 3 keeps one out-of-line copy of each larger
-// two-float routine (logarithm, exponential, e^(ix), complex inverse, argument).
+// two-float routine (logarithm, exponential, e^(ix), complex inverse, argument), bit 4
+// of the complex two-float product and multiply-add.
 #ifndef FT_VARIANT
 #define FT_VARIANT 0
 #endif
@@ -84,6 +85,11 @@ typedef unsigned int u32;
 #define FT_BIGFN __noinline__
 #else
 #define FT_BIGFN __forceinline__
+#endif
+#if (FT_VARIANT & 16) && !defined(FT_HOST_SIM)
+#define FT_CXFN __noinline__
+#else
+#define FT_CXFN __forceinline__
 #endif
 static __device__ FT_MATHFN float m_log1p(float x) { return log1pf(x); }
 static __device__ FT_MATHFN float m_exp(float x) { return expf(x); }
@@ -1206,7 +1212,7 @@ static __device__ __forceinline__ cdf cdf_mk(df r, df i)
 static __device__ __forceinline__ cdf cdf_zero() { return cdf_mk(df_mk(0.0f), df_mk(0.0f)); }
 static __device__ __forceinline__ cdf operator+(cdf a, cdf b) { return cdf_mk(df_add(a.re, b.re), df_add(a.im, b.im)); }
 static __device__ __forceinline__ cdf operator-(cdf a, cdf b) { return cdf_mk(df_sub(a.re, b.re), df_sub(a.im, b.im)); }
-static __device__ __forceinline__ cdf operator*(cdf a, cdf b)
+static __device__ FT_CXFN cdf operator*(cdf a, cdf b)
 {
     return cdf_mk(df_fma(a.re, b.re, df_neg(df_mul(a.im, b.im))), df_fma(a.re, b.im, df_mul(a.im, b.re)));
 }
@@ -1217,7 +1223,7 @@ static __device__ FT_BIGFN cdf cdf_inv(cdf a)
     return cdf_mk(df_mul(a.re, m), df_neg(df_mul(a.im, m)));
 }
 // a b + c with four two-float FMAs
-static __device__ __forceinline__ cdf cdf_fma(cdf a, cdf b, cdf c)
+static __device__ FT_CXFN cdf cdf_fma(cdf a, cdf b, cdf c)
 {
     return cdf_mk(df_fma(a.re, b.re, df_fma(df_neg(a.im), b.im, c.re)), df_fma(a.re, b.im, df_fma(a.im, b.re, c.im)));
 }
