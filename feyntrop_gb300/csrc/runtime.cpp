@@ -842,14 +842,15 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
             cands.push_back(s);
         };
         if (prec == 1 && deformed) {
-            // two-float determinant and V: out-of-line routines (bit 3) and shapes from 128
-            // registers (16 warps per SM) to 255 (8 warps, no spills)
-            for (int var : {13, 5}) {
-                add(512, 1, var);
-                add(256, 2, var);
-                add(256, 1, var);
-            }
-            add(384, 1, 13);
+            // two-float determinant and V: out-of-line two-float routines (bits 3, 4) and
+            // shapes from 128 registers (16 warps per SM) to 255 (8 warps, no spills)
+            add(256, 2, 29);
+            add(512, 1, 29);
+            add(128, 4, 29);
+            add(384, 1, 29);
+            add(256, 1, 29);
+            add(512, 1, 13);
+            add(256, 1, 13);
         } else if (prec == 1) {
             for (int var : {4, 0})
                 for (int bm : {512, 256, 128}) add(bm, 512 / bm, var);

@@ -85,22 +85,24 @@ launch_shape default_shape(const kernel_key& k)
     // GB300 sweeps (double box, box-pentagon, 3-loop ladder, K4, cube): the mixed form is
     // bound by instruction fetch and gains 15-25 % from blocks whose warps start each
     // sample together (variant bit 2).  Deformed integrands, whose determinant and V run
-    // in two-float, also gain from out-of-line FP32 transcendentals (bit 0) and two-float
-    // routines (bit 3, +5 %); up to 7 edges they run best as one 384-thread block per SM
-    // (168 registers; double box 1.17e9 samples/s against 1.11e9 for 512 x 1 and 1.05e9
-    // for two 256-thread blocks), from 8 edges as one 256-thread block with 255 registers
-    // (no spills: box-pentagon +6 %, 3-loop ladder +25 % over 512 x 1).  Undeformed
-    // integrands keep one 512-thread block.  The FP64 form is FP64-pipe bound (256 x 1); the per-sample
-    // barrier keeps its warps from drifting apart too (cube +10 %, double box +1 %).
+    // in two-float, gain most from a smaller code: one out-of-line copy of the FP32
+    // transcendentals (bit 0), of the larger two-float routines (bit 3) and of the
+    // complex two-float product and multiply-add (bit 4: +37 % on the double box, +82 %
+    // on the box-pentagon).  With it they run best as two 256-thread blocks per SM
+    // (128 registers; double box 1.59e9 samples/s, 3-loop ladder 7.2e8; the box-pentagon
+    // 0.94e9 against 1.01e9 for 512 x 1).  Out-of-line two-float add and multiply (bit 1)
+    // cost 45 %.  Undeformed integrands keep one 512-thread block.  The FP64 form is
+    // FP64-pipe bound (256 x 1); the per-sample barrier keeps its warps from drifting
+    // apart too (cube +10 %, double box +1 %).
     launch_shape s;
     if (k.prec == 1) {
-        s.block = k.mode == 1 ? (k.E >= 8 ? 256 : 384) : 512;
-        s.minb = 1;
+        s.block = k.mode == 1 ? 256 : 512;
+        s.minb = k.mode == 1 ? 2 : 1;
     } else {
         s.block = 256;
         s.minb = 1;
     }
-    s.variant = (k.prec == 1 && k.mode == 1) ? 13 : (k.mode == 1 ? 5 : 4);
+    s.variant = (k.prec == 1 && k.mode == 1) ? 29 : (k.mode == 1 ? 5 : 4);
     return s;
 }
 
