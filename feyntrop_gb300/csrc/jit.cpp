@@ -83,6 +83,41 @@ static std::string tables_source()
     return text;
 }
 
+// Structural pattern of the conductance-form elimination of the reduced Laplacian (the
+// deleted vertex is V-1): nz[i*n+j] (i < j) marks a conductance between i and j that is
+// non-zero when vertex i is eliminated (an edge, or fill from an earlier elimination),
+// nzg[i] a conductance to ground, nzm[i*n+j] an entry of M^-1 (M the unit upper
+// triangular factor) that can be non-zero.  The kernels skip every update on a
+// structural zero (a compiler cannot drop x + 0 * y in IEEE arithmetic).
+static void elimination_pattern(const kernel_key& k, std::vector<int>& nz, std::vector<int>& nzg,
+                                std::vector<int>& nzm)
+{
+    const int n = k.V - 1;
+    nz.assign((size_t)n * n, 0);
+    nzg.assign(n, 0);
+    nzm.assign((size_t)n * n, 0);
+    for (int e = 0; e < k.E; e++) {
+        const int a = k.ek[e], b = k.el[e];   // a > b
+        if (a == k.V - 1)
+            nzg[b] = 1;
+        else
+            nz[b * n + a] = 1;
+    }
+    for (int kk = 0; kk < n; kk++)
+        for (int i = kk + 1; i < n; i++) {
+            if (!nz[kk * n + i]) continue;
+            if (nzg[kk]) nzg[i] = 1;
+            for (int j = i + 1; j < n; j++)
+                if (nz[kk * n + j]) nz[i * n + j] = 1;
+        }
+    for (int i = n - 1; i >= 0; i--)
+        for (int j = i + 1; j < n; j++) {
+            int v = nz[i * n + j];
+            for (int m = i + 1; m < j && !v; m++) v = nz[i * n + m] && nzm[m * n + j];
+            nzm[i * n + j] = v;
+        }
+}
+
 std::string kernel_source(const kernel_key& k)
 {
     std::ostringstream s;
@@ -100,6 +135,25 @@ std::string kernel_source(const kernel_key& k)
     s << "};\n__device__ constexpr int FT_EL[" << k.E << "] = {";
     for (int e = 0; e < k.E; e++) s << (e ? "," : "") << k.el[e];
     s << "};\n";
+    {
+        std::vector<int> nz, nzg, nzm;
+        elimination_pattern(k, nz, nzg, nzm);
+        const int n = k.V - 1;
+        auto matrix = [&](const char* name, const std::vector<int>& m) {
+            s << "__device__ constexpr unsigned char " << name << "[" << n << "][" << n << "] = {";
+            for (int i = 0; i < n; i++) {
+                s << "{";
+                for (int j = 0; j < n; j++) s << (j ? "," : "") << m[i * n + j];
+                s << "},";
+            }
+            s << "};\n";
+        };
+        matrix("FT_NZC", nz);
+        matrix("FT_NZM", nzm);
+        s << "__device__ constexpr unsigned char FT_NZG[" << n << "] = {";
+        for (int i = 0; i < n; i++) s << (i ? "," : "") << nzg[i];
+        s << "};\n#define FT_HAVE_PATTERN 1\n";
+    }
     s << tables_source();
     s << ft_sample_body_source;
     return s.str();

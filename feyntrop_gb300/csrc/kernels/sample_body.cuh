@@ -107,6 +107,19 @@ static __device__ FT_MATHFN float m_atan(float x) { return atanf(x); }
 #ifndef FT_Q0
 #define FT_Q0 0
 #endif
+// Structural pattern of the eliminations, generated per topology: NZC(i, j) (i < j) a
+// conductance between i and j that can be non-zero when i is eliminated (an edge or
+// fill), NZG(i) a conductance to ground, NZM(i, j) an entry of M^-1 that can be
+// non-zero.  Updates on structural zeros are left out (without the tables: dense).
+#ifdef FT_HAVE_PATTERN
+#define NZC(i, j) (FT_NZC[i][j] != 0)
+#define NZG(i) (FT_NZG[i] != 0)
+#define NZM(i, j) (FT_NZM[i][j] != 0)
+#else
+#define NZC(i, j) true
+#define NZG(i) true
+#define NZM(i, j) true
+#endif
 #define FT_FULL ((1u << FT_E) - 1u)
 #define FT_NPAIR (FT_E * (FT_E - 1) / 2)
 
@@ -279,6 +292,7 @@ struct elim {
             R mag = mag_of(g[k]);
 #pragma unroll
             for (int j = k + 1; j < FT_N; j++) {
+                if (!NZC(k, j)) continue;
                 dk = dk + c[k][j];
                 mag += mag_of(c[k][j]);
             }
@@ -287,12 +301,14 @@ struct elim {
             worst = ratio < worst ? ratio : worst;
             F inv = inv_of(dk);
 #pragma unroll
-            for (int i = k + 1; i < FT_N; i++) a[k][i] = c[k][i] * inv;
+            for (int i = k + 1; i < FT_N; i++) a[k][i] = NZC(k, i) ? c[k][i] * inv : F{};
 #pragma unroll
             for (int i = k + 1; i < FT_N; i++) {
-                g[i] = g[i] + a[k][i] * g[k];
+                if (!NZC(k, i)) continue;
+                if (NZG(k)) g[i] = g[i] + a[k][i] * g[k];
 #pragma unroll
-                for (int j = i + 1; j < FT_N; j++) c[i][j] = c[i][j] + a[k][i] * c[k][j];
+                for (int j = i + 1; j < FT_N; j++)
+                    if (NZC(k, j)) c[i][j] = c[i][j] + a[k][i] * c[k][j];
             }
         }
         return worst;
@@ -309,7 +325,8 @@ struct elim {
         for (int i = FT_Q0; i < FT_N; i++) {
             F yi = from_real((R)q[i]);
 #pragma unroll
-            for (int k = FT_Q0; k < i; k++) yi = yi + a[k][i] * y[k];
+            for (int k = FT_Q0; k < i; k++)
+                if (NZC(k, i)) yi = yi + a[k][i] * y[k];
             y[i] = yi;
             s = s + yi * yi * inv_of(d[i]);
         }
@@ -326,7 +343,8 @@ struct elim {
         for (int i = FT_Q0; i < FT_N; i++) {
             F yi = from_real((R)q[i]);
 #pragma unroll
-            for (int k = FT_Q0; k < i; k++) yi = yi + a[k][i] * y[k];
+            for (int k = FT_Q0; k < i; k++)
+                if (NZC(k, i)) yi = yi + a[k][i] * y[k];
             y[i] = yi;
             const F t = yi * yi * inv_of(d[i]);
             s = s + t;
@@ -959,9 +977,11 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
         Nm[i][i] = 1.0;
 #pragma unroll
         for (int j = i + 1; j < FT_N; j++) {
+            if (!NZM(i, j)) continue;
             double s = 0.0;
 #pragma unroll
-            for (int k = i + 1; k <= j; k++) s += L.a[i][k] * Nm[k][j];
+            for (int k = i + 1; k <= j; k++)
+                if (NZC(i, k) && (k == j || NZM(k, j))) s += L.a[i][k] * Nm[k][j];
             Nm[i][j] = s;
         }
     }
@@ -975,7 +995,8 @@ static __device__ __forceinline__ bool integrand64(const double* prm, double* X,
         for (int j = i; j < FT_N; j++) {
             double s = 0.0;
 #pragma unroll
-            for (int k = j; k < FT_N; k++) s += Nm[i][k] * Nm[j][k] * id[k];
+            for (int k = j; k < FT_N; k++)
+                if ((k == i || NZM(i, k)) && (k == j || NZM(j, k))) s += Nm[i][k] * Nm[j][k] * id[k];
             G[i][j] = s;
             G[j][i] = s;
         }
@@ -1155,13 +1176,19 @@ static __device__ __forceinline__ df df_neg(df x)
     return x;
 }
 static __device__ __forceinline__ df df_sub(df x, df y) { return df_add(x, df_neg(y)); }
+// A product cannot cancel: its low part e stays within ~1.5 ulp of p, which every
+// consumer (sums, products, the reciprocal, conversions) handles, so it is returned
+// without renormalisation.
 static __device__ FT_DFFN df df_mul(df x, df y)
 {
     const float p = x.hi * y.hi;
     float e = fmaf(x.hi, y.hi, -p);
     e = fmaf(x.hi, y.lo, e);
     e = fmaf(x.lo, y.hi, e);
-    return df_norm(p, e);
+    df r;
+    r.hi = p;
+    r.lo = e;
+    return r;
 }
 // x y + z: the leading product exact (FMA residual), one two-sum with z.hi, the small
 // terms added once
@@ -1178,10 +1205,14 @@ static __device__ FT_DFFN df df_fma(df x, df y, df z)
 static __device__ FT_DFFN df df_inv(df x)
 {
     // one Newton step from the FP32 reciprocal r: 1/x = r (1 + e) with e = 1 - x r;
-    // 1 - x.hi r (about 2^-23) is exact to 2^-47 by the FMA, then x.lo r is removed
+    // 1 - x.hi r (about 2^-23) is exact to 2^-47 by the FMA, then x.lo r is removed.
+    // |r e| stays within about an ulp of r, so the pair needs no renormalisation.
     const float r = rcp_(x.hi);
     const float e = fmaf(-x.lo, r, fmaf(-x.hi, r, 1.0f));
-    return df_norm(r, r * e);
+    df o;
+    o.hi = r;
+    o.lo = r * e;
+    return o;
 }
 static __device__ __forceinline__ float df_f(df x) { return x.hi + x.lo; }
 static __device__ __forceinline__ df df_of(f2 x)
@@ -1332,6 +1363,7 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
         float row = cmag_hi(g[k]);
 #pragma unroll
         for (int j = k + 1; j < FT_N; j++) {
+            if (!NZC(k, j)) continue;
             dk = dk + c[k][j];
             row += cmag_hi(c[k][j]);
         }
@@ -1340,12 +1372,15 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
         ok &= cdf_renorm(det, det_e);
         dinv[k] = cdf_inv(dk);
 #pragma unroll
-        for (int i = k + 1; i < FT_N; i++) a[k][i] = c[k][i] * dinv[k];
+        for (int i = k + 1; i < FT_N; i++)
+            if (NZC(k, i)) a[k][i] = c[k][i] * dinv[k];
 #pragma unroll
         for (int i = k + 1; i < FT_N; i++) {
-            g[i] = cdf_fma(a[k][i], g[k], g[i]);
+            if (!NZC(k, i)) continue;
+            if (NZG(k)) g[i] = cdf_fma(a[k][i], g[k], g[i]);
 #pragma unroll
-            for (int j = i + 1; j < FT_N; j++) c[i][j] = cdf_fma(a[k][i], c[k][j], c[i][j]);
+            for (int j = i + 1; j < FT_N; j++)
+                if (NZC(k, j)) c[i][j] = cdf_fma(a[k][i], c[k][j], c[i][j]);
         }
     }
     float qmag = 0.0f;
@@ -1358,7 +1393,8 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
         for (int i = FT_Q0; i < FT_N; i++) {
             cdf yi = cdf_mk(pdf(P_Q + r * FT_N + i), df_mk(0.0f));
 #pragma unroll
-            for (int k = FT_Q0; k < i; k++) yi = cdf_fma(a[k][i], yv[k], yi);
+            for (int k = FT_Q0; k < i; k++)
+                if (NZC(k, i)) yi = cdf_fma(a[k][i], yv[k], yi);
             yv[i] = yi;
             const cdf t = (yi * yi) * dinv[i];
             qm += cmag_hi(t);
@@ -1409,15 +1445,19 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
     for (int k = 0; k < FT_N; k++) {
         df dk = g[k];
 #pragma unroll
-        for (int j = k + 1; j < FT_N; j++) dk = df_add(dk, c[k][j]);
+        for (int j = k + 1; j < FT_N; j++)
+            if (NZC(k, j)) dk = df_add(dk, c[k][j]);
         id[k] = df_inv(dk);
 #pragma unroll
-        for (int i = k + 1; i < FT_N; i++) a[k][i] = df_mul(c[k][i], id[k]);
+        for (int i = k + 1; i < FT_N; i++)
+            if (NZC(k, i)) a[k][i] = df_mul(c[k][i], id[k]);
 #pragma unroll
         for (int i = k + 1; i < FT_N; i++) {
-            g[i] = df_fma(a[k][i], g[k], g[i]);
+            if (!NZC(k, i)) continue;
+            if (NZG(k)) g[i] = df_fma(a[k][i], g[k], g[i]);
 #pragma unroll
-            for (int j = i + 1; j < FT_N; j++) c[i][j] = df_fma(a[k][i], c[k][j], c[i][j]);
+            for (int j = i + 1; j < FT_N; j++)
+                if (NZC(k, j)) c[i][j] = df_fma(a[k][i], c[k][j], c[i][j]);
         }
     }
     // N = M^-1 (unit upper triangular, non-negative), G = N diag(1/d) N^T
@@ -1426,9 +1466,11 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
     for (int i = FT_N - 1; i >= 0; i--) {
 #pragma unroll
         for (int j = i + 1; j < FT_N; j++) {
-            df s = a[i][j];
+            if (!NZM(i, j)) continue;
+            df s = NZC(i, j) ? a[i][j] : df_mk(0.0f);
 #pragma unroll
-            for (int k = i + 1; k < j; k++) s = df_fma(a[i][k], Nm[k][j], s);
+            for (int k = i + 1; k < j; k++)
+                if (NZC(i, k) && NZM(k, j)) s = df_fma(a[i][k], Nm[k][j], s);
             Nm[i][j] = s;
         }
     }
@@ -1438,9 +1480,10 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
 #pragma unroll
         for (int j = i; j < FT_N; j++) {
             // k = j term has N[j][j] = 1
-            df s = (i == j) ? id[j] : df_mul(Nm[i][j], id[j]);
+            df s = (i == j) ? id[j] : (NZM(i, j) ? df_mul(Nm[i][j], id[j]) : df_mk(0.0f));
 #pragma unroll
-            for (int k = j + 1; k < FT_N; k++) s = df_fma(df_mul(Nm[i][k], Nm[j][k]), id[k], s);
+            for (int k = j + 1; k < FT_N; k++)
+                if (NZM(i, k) && NZM(j, k)) s = df_fma(df_mul(Nm[i][k], Nm[j][k]), id[k], s);
             G[i][j] = s;
             G[j][i] = s;
         }
