@@ -120,6 +120,14 @@ static __device__ FT_MATHFN float m_atan(float x) { return atanf(x); }
 #define NZG(i) true
 #define NZM(i, j) true
 #endif
+// edge e is the first to contribute to its conductance slot (the pair of endpoints, or
+// the ground slot of its lower endpoint): its conductance is assigned, not added to zero
+static __device__ constexpr bool first_in_slot(int e)
+{
+    for (int f = 0; f < e; f++)
+        if (FT_EK[f] == FT_EK[e] && FT_EL[f] == FT_EL[e]) return false;
+    return true;
+}
 #define FT_FULL ((1u << FT_E) - 1u)
 #define FT_NPAIR (FT_E * (FT_E - 1) / 2)
 
@@ -280,10 +288,8 @@ struct elim {
 #pragma unroll
         for (int e = 0; e < FT_E; e++) {
             const int k = FT_EK[e], l = FT_EL[e];
-            if (k == FT_V - 1)
-                g[l] = g[l] + y[e];
-            else
-                c[l][k] = c[l][k] + y[e];
+            F& slot = (k == FT_V - 1) ? g[l] : c[l][k];
+            slot = first_in_slot(e) ? y[e] : slot + y[e];
         }
         R worst = R(1);
 #pragma unroll
@@ -1344,12 +1350,11 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
         const df xi = df_of(Xi2[e]);
         const cdf y = cdf_mk(df_mul(xi, cs), df_neg(df_mul(xi, sn)));
         const int k = FT_EK[e], l = FT_EL[e];
-        if (k == FT_V - 1)
-            g[l] = g[l] + y;
-        else
-            c[l][k] = c[l][k] + y;
+        cdf& slot = (k == FT_V - 1) ? g[l] : c[l][k];
+        slot = first_in_slot(e) ? y : slot + y;
         const df m2x = df_mul(pdf(P_M2 + e), df_inv(xi));
-        v = v + cdf_mk(df_mul(m2x, cs), df_mul(m2x, sn));
+        const cdf mt = cdf_mk(df_mul(m2x, cs), df_mul(m2x, sn));
+        v = e == 0 ? mt : v + mt;
         mag += fabsf(m2x.hi);
     }
     cdf a[FT_N][FT_N], dinv[FT_N];
@@ -1398,7 +1403,7 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
             yv[i] = yi;
             const cdf t = (yi * yi) * dinv[i];
             qm += cmag_hi(t);
-            sr = sr + t;
+            sr = i == FT_Q0 ? t : sr + t;
         }
         const df sg = pdf(P_SIG + r);
         v = v - sg * sr;
@@ -1435,10 +1440,8 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
 #pragma unroll
     for (int e = 0; e < FT_E; e++) {
         const int k = FT_EK[e], l = FT_EL[e];
-        if (k == FT_V - 1)
-            g[l] = df_add(g[l], df_of(XiT[e]));
-        else
-            c[l][k] = df_add(c[l][k], df_of(XiT[e]));
+        df& slot = (k == FT_V - 1) ? g[l] : c[l][k];
+        slot = first_in_slot(e) ? df_of(XiT[e]) : df_add(slot, df_of(XiT[e]));
     }
     df a[FT_N][FT_N], id[FT_N];
 #pragma unroll
@@ -1468,9 +1471,13 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
         for (int j = i + 1; j < FT_N; j++) {
             if (!NZM(i, j)) continue;
             df s = NZC(i, j) ? a[i][j] : df_mk(0.0f);
+            bool any = NZC(i, j);
 #pragma unroll
             for (int k = i + 1; k < j; k++)
-                if (NZC(i, k) && NZM(k, j)) s = df_fma(a[i][k], Nm[k][j], s);
+                if (NZC(i, k) && NZM(k, j)) {
+                    s = any ? df_fma(a[i][k], Nm[k][j], s) : df_mul(a[i][k], Nm[k][j]);
+                    any = true;
+                }
             Nm[i][j] = s;
         }
     }
@@ -1499,7 +1506,7 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
                 df q;
                 q.hi = pd[2 * (P_Q + r * FT_N + j)];
                 q.lo = pd[2 * (P_Q + r * FT_N + j) + 1];
-                s = df_fma(G[i][j], q, s);
+                s = j == FT_Q0 ? df_mul(G[i][j], q) : df_fma(G[i][j], q, s);
             }
             h[i] = s;
         }
@@ -1510,6 +1517,23 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
         }
     }
     auto Gx = [&](int i, int j) -> df { return (i == FT_V - 1 || j == FT_V - 1) ? df_mk(0.0f) : G[i][j]; };
+    // (G_pq + G_rs) - (G_pt + G_uv) over the terms without the ground vertex (its row of
+    // L^-1 is zero), so that no zero is added
+    auto gcomb = [&](int p1, int q1, int p2, int q2, int m1, int n1, int m2, int n2) -> df {
+        df acc = df_mk(0.0f);
+        bool any = false;
+        auto put = [&](int i, int j, bool neg) {
+            if (i == FT_V - 1 || j == FT_V - 1) return;
+            const df v = neg ? df_neg(G[i][j]) : G[i][j];
+            acc = any ? df_add(acc, v) : v;
+            any = true;
+        };
+        put(p1, q1, false);
+        put(p2, q2, false);
+        put(m1, n1, true);
+        put(m2, n2, true);
+        return acc;
+    };
     df kappa;
     kappa.hi = pd[2 * P_DEF];
     kappa.lo = pd[2 * P_DEF + 1];
@@ -1524,9 +1548,9 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
             sg.hi = pd[2 * (P_SIG + r)];
             sg.lo = pd[2 * (P_SIG + r) + 1];
             sig_hb[r] = df_mul(sg, hb[r][a2]);
-            s = df_fma(sig_hb[r], hb[r][a2], s);
+            s = r == 0 ? df_mul(sig_hb[r], hb[r][a2]) : df_fma(sig_hb[r], hb[r][a2], s);
         }
-        const df t = df_sub(df_add(Gx(ka, ka), Gx(la, la)), df_add(Gx(ka, la), Gx(ka, la)));
+        const df t = gcomb(ka, ka, la, la, ka, la, ka, la);
         // an edge whose ends float together: the FP64 pass takes the sample
         cancel |= ka != FT_V - 1 && !(df_f(t) > 1e-7f * (df_f(Gx(ka, ka)) + df_f(Gx(la, la))));
         const df xi = df_of(XiT[a2]);
@@ -1543,8 +1567,8 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
             const int kb = FT_EK[b], lb = FT_EL[b];
             df s2 = df_mk(0.0f);
 #pragma unroll
-            for (int r = 0; r < FT_RANK; r++) s2 = df_fma(sig_hb[r], hb[r][b], s2);
-            const df t2 = df_sub(df_add(Gx(ka, kb), Gx(la, lb)), df_add(Gx(ka, lb), Gx(la, kb)));
+            for (int r = 0; r < FT_RANK; r++) s2 = r == 0 ? df_mul(sig_hb[r], hb[r][b]) : df_fma(sig_hb[r], hb[r][b], s2);
+            const df t2 = gcomb(ka, kb, la, lb, ka, lb, la, kb);
             const float xb = Xi32[b];
             H_out[a2][b] = -2.0f * df_f(df_mul(xa, df_mk(xb * xb))) * df_f(s2) * df_f(t2);
         }
