@@ -844,9 +844,10 @@ int ft_autotune(ft_plan* pl, int32_t precision, uint64_t samples, ft_tune_result
         if (prec == 1 && deformed) {
             // two-float determinant and V: out-of-line two-float routines (bits 3, 4) and
             // shapes from 128 registers (16 warps per SM) to 255 (8 warps, no spills)
+            // (four 128-thread blocks won one-integral trials by noise and ran the
+            // persistent batch kernel 9 % slower: not a candidate)
             add(256, 2, 29);
             add(512, 1, 29);
-            add(128, 4, 29);
             add(384, 1, 29);
             add(256, 1, 29);
             add(512, 1, 13);

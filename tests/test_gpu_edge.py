@@ -94,3 +94,39 @@ def test_batch_with_an_empty_integral():
     assert abs(x - r["integral"][0][0][0]) <= 1e-3 * dx
     for p in ps:
         p.close()
+
+
+def relabelled(inp, perm):
+    """The same Feynman graph with vertex v renamed perm[v] (edges in the same order)."""
+    V = len(inp["scalarproducts"])
+    P = [[0.0] * V for _ in range(V)]
+    for i in range(V):
+        for j in range(V):
+            P[perm[i]][perm[j]] = inp["scalarproducts"][i][j]
+    graph = [[[perm[a], perm[b]], nu] for (a, b), nu in inp["graph"]]
+    return dict(inp, graph=graph, scalarproducts=P)
+
+
+@pytest.mark.parametrize("name,perm", [("C2_double_box", [5, 3, 0, 4, 1, 2]),
+                                       ("C3_box_pentagon_0", [6, 0, 5, 1, 4, 2, 3]),
+                                       ("ladder3_4pt_mink", [7, 6, 5, 4, 3, 2, 1, 0])])
+def test_vertex_labels_do_not_change_the_samples(name, perm):
+    """The kernels relabel the vertices (internal ones first, the deleted one external)
+    and skip the eliminations' structural zeros from each topology's fill pattern; the
+    integrand does not depend on the labels, so a renamed graph (here with its external
+    vertices moved among the internal ones) gives the same sectors and, per sample, the
+    same values to rounding: FP64 to 1e-10 for 99.9 % of the samples (ill-conditioned
+    sectors, where the deleted vertex changes the rounding most, to 1e-6), the mixed
+    form within its 1e-5 bound of FP64 on either side."""
+    inp = PINS["cases"][name]["input"]
+    a, b = ft.Plan(inp), ft.Plan(relabelled(inp, perm))
+    for prec, tol, tol999 in ((ft.FP64, 1e-6, 1e-10), (ft.MIXED, 2e-5, 5e-6)):
+        ra = a.records(4096, seed=3, precision=prec)
+        rb = b.records(4096, seed=3, precision=prec)
+        assert (ra["order"] == rb["order"]).all()
+        ok = ((ra["flags"] | rb["flags"]) & 1) == 0
+        scale = np.abs(ra["R"][ok]).max(axis=1)
+        err = np.abs(ra["R"][ok] - rb["R"][ok]).max(axis=1) / np.where(scale > 0, scale, 1.0)
+        assert np.quantile(err, 0.999) < tol999 and err.max() < tol, (prec, np.quantile(err, 0.999), err.max())
+    a.close()
+    b.close()
