@@ -452,7 +452,9 @@ int ft_batch_run(ft_batch* b, const ft_run_options* opts, ft_result* results)
                 p->first_item = next;
                 p->nitems = items;
                 next += items;
-                q += (size_t)std::min<unsigned long long>(N, N / 64 + 1024);
+                // hand-offs run at ~1e-5 of the samples; a larger share overflows the
+                // queue, which then grows and the run repeats once
+                q += (size_t)std::min<unsigned long long>(N, N / 1024 + 1024);
             }
             if (next >= (1ull << 36)) throw std::invalid_argument("ft_batch_run: too many work items");
             g.total_items = next;
