@@ -1,9 +1,10 @@
 """Regenerates tests/golden/reference_pins.json from the reference itself.
 
-Run in a checkout where the reference sources exist (default /root/reference,
-override with FEYNTROP_REFERENCE) after `make -C oracle ref`:
+Run with FEYNTROP_REFERENCE naming a checkout of the reference's sources, after
+`make -C oracle ref REF=$FEYNTROP_REFERENCE`:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py                # every case
+    python tests/golden/make_golden.py --only NAME..  # these cases, merged into the pins
 
 For every case below it records, from the reference build (oracle/_ref):
   * the J(gamma) table of generate_subgraph_table (full table as IEEE bit patterns
