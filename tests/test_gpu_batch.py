@@ -120,6 +120,25 @@ def test_sharded_batch_blocks_merge_to_one_run(plans):
     b.close()
 
 
+@pytest.mark.parametrize("mode", ["samples", "integrals"])
+def test_run_sharded_on_one_rank_equals_run(plans, mode):
+    """Batch.run_sharded with a single rank (no process group needed) takes the sharded
+    path end to end and returns the whole batch's results: the same counts and, to
+    rounding, the same integrals as Batch.run."""
+    b = ft.Batch(plans, ft.FP64)
+    Ns = [200_000 + 1000 * i for i in range(len(plans))]
+    full = b.run(Ns, seeds=4)
+    sh = b.run_sharded(Ns, rank=0, world=1, seeds=4, mode=mode)
+    for i, p in enumerate(plans):
+        assert sh[i]["samples"] == Ns[i]
+        assert [m[0] for m in sh[i]["moments"]] == [m[0] for m in full[i]["moments"]], NAMES[i]
+        for j, ((re, dre), (im, dim)) in enumerate(full[i]["integral"]):
+            (sre, sdre), (sim, sdim) = sh[i]["integral"][j]
+            assert abs(sre - re) <= 1e-9 * max(dre, 1e-300) and abs(sdre - dre) <= 1e-9 * dre, (NAMES[i], j)
+            assert abs(sim - im) <= 1e-9 * max(dim, 1e-300) or (dim == 0 and sim == 0), (NAMES[i], j)
+    b.close()
+
+
 def test_batch_runs_are_bit_identical():
     """The FP64 pass of a mixed batch adds its samples into exact fixed-point
     accumulators, so the order in which the queue's entries are handled does not
