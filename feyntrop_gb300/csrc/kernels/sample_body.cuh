@@ -24,9 +24,11 @@
 //    is bit-identical.  The mixed form decides each comparison in FP32 with a
 //    rigorous error margin and repeats the scan in FP64 when a comparison falls
 //    inside the margin.  The mixed form keeps log X in a two-float sum.
-//  * The deleted vertex of the reduced Laplacian is always the last one.  Any choice
-//    gives the same psi, phi/psi and derivatives (matrix-tree theorem and momentum
-//    conservation); the reference's choice only affects rounding.
+//  * The deleted vertex of the reduced Laplacian is always the last one of the
+//    kernel's labels (the host numbers the vertices without external momentum first,
+//    so it is an external one).  Any choice gives the same psi, phi/psi and
+//    derivatives (matrix-tree theorem and momentum conservation); the reference's
+//    choice only affects rounding.
 //  * The real reduced Laplacian is eliminated in conductance form: pivots are sums
 //    of positive conductances and updates add positive products, so psi = det L *
 //    prod X has full relative accuracy whatever the spread of X.
@@ -34,11 +36,14 @@
 //    each term is a forward substitution with the elimination multipliers.
 //  * Deformed branch: L^-1 from the positive factors, x-derivatives of phi/psi
 //    (srcs/laplacian.hpp:102-215), the complex Laplacian eliminated in the same
-//    conductance form with a pivot-growth check (samples failing it take a
-//    complete-pivoting LU, srcs/feynman_integral.hpp:305), and the Jacobian
-//    determinant as det(I + i*lambda' X^1/2 H X^1/2) (similar to
+//    conductance form with a pivot-growth check (the FP64 form's failing samples take
+//    a complete-pivoting LU, srcs/feynman_integral.hpp:305; the mixed form runs this
+//    elimination and V in two-float and hands the rare failing samples to FP64), and
+//    the Jacobian determinant as det(I + i*lambda' X^1/2 H X^1/2) (similar to
 //    I + i*lambda' H X, srcs/feynman_integral.hpp:312), whose real part is the
 //    identity, so symmetric elimination without pivoting is stable.
+//  * Updates on structural zeros of the eliminations (from each topology's fill
+//    pattern, generated by the host) and additions to zero are left out.
 
 #ifndef FT_E
 #error "topology constants missing"
