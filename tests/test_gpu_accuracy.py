@@ -36,7 +36,7 @@ def accept(inp):
 
 def test_double_box_tail():
     p = ft.Plan(workloads.double_box())
-    e, queued = errors(p, 1 << 18)
+    e, queued = errors(p, 1 << 20)
     assert e.max() <= TOL, np.sort(e)[-5:]
     assert np.quantile(e, 0.999) <= 3e-6
     assert np.median(e) < 1e-6
@@ -49,7 +49,7 @@ def test_random_box_pentagon_tail():
     es, qs = [], []
     for inp in inputs:
         p = ft.Plan(inp)
-        e, q = errors(p, 8192, seed=2)
+        e, q = errors(p, 32768, seed=2)
         es.append(e)
         qs.append(q)
         p.close()
