@@ -108,9 +108,10 @@ struct ft_plan {
         k.ek = kek;
         k.el = kel;
         k.q0 = q0;
-        // small tables are staged per block in shared memory; from E = 11 on the table is
-        // read through L1 (one cached copy per SM instead of one per block)
-        k.table_global = P.E >= 11 ? 1 : 0;
+        // tables are staged per block in shared memory up to E = 12 (102 KB FP64, 70 KB
+        // mixed, beside one block's per-thread sums: the cube's mixed kernel ran 8 % faster
+        // than reading its table through L1); from E = 13 on they are read through L1
+        k.table_global = P.E >= 13 ? 1 : 0;
         // launch shape: a shape being measured by the autotuner, else the tuning table's
         // (or the default) for this kernel class
         ft::apply_shape(k, (forced && forced_prec == prec) ? forced_shape : ft::choose_shape(k));
