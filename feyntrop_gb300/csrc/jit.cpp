@@ -28,11 +28,13 @@ static const char* kArch = "--gpu-architecture=sm_103a";
 
 unsigned table_smem_bytes(const kernel_key& k)
 {
-    // staged table (unless read from global memory), then the per-thread accumulators
+    // staged table (unless read from global memory), then the per-thread accumulators:
+    // FP64 form two doubles per slot; mixed form two doubles and two floats per slot and
+    // four sample counters (a double and a float each)
     const unsigned entries = 1u << k.E;
     const unsigned tab = k.table_global ? 0u : (k.prec == 0 ? 25u * entries : 17u * entries);
     const unsigned parts = k.mode == 1 ? 4u : 2u;
-    const unsigned acc = (unsigned)k.block * parts * (unsigned)k.K * (k.prec == 0 ? 16u : 24u);
+    const unsigned acc = (unsigned)k.block * (parts * (unsigned)k.K * (k.prec == 0 ? 16u : 24u) + (k.prec == 0 ? 0u : 48u));
     return ((tab + 15u) & ~15u) + acc;
 }
 

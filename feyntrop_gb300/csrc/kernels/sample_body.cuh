@@ -648,6 +648,23 @@ struct table_ref {
     const unsigned char* gm;    // global copy (FP64 sections for exact re-checks)
 };
 
+#if FT_BATCH
+// The batch kernels' current work item and its instance's table (global copy), written
+// by the block's first thread between items and read where they are used, so that
+// neither is held in registers across the per-sample code.
+__shared__ unsigned long long s_batch_item;
+__shared__ const unsigned char* s_batch_tab;
+#define TABLE_GM(t) s_batch_tab
+// first word of an FP64-pass queue entry: item << 28 | lane << 18 | offset of the
+// sample in the lane's chunk (the other four hold the sample's stream state)
+#define BQ_ITEM_SHIFT 28
+#define BQ_LANE_SHIFT 18
+#define BQ_OFF_MASK ((1ull << BQ_LANE_SHIFT) - 1ull)
+#define BQ_LANE_MASK 1023ull
+#else
+#define TABLE_GM(t) ((t).gm)
+#endif
+
 static __device__ __forceinline__ void draw_sector64(xo& g, const table_ref& t, double Jr_full, double* X, double& F,
                                                      double& Gv, unsigned char* ord)
 {
@@ -887,7 +904,7 @@ static __device__ __forceinline__ int draw_sector32(xo& g, const table_ref& t, c
         }
         int cut = sure >= 0 ? sure : e;
         if (unsure) {
-            cut = exact_cut(x, sub, t.gm);
+            cut = exact_cut(x, sub, TABLE_GM(t));
             exact++;
         }
         sub ^= 1u << cut;
@@ -2098,12 +2115,13 @@ static __device__ __forceinline__ void copy_bytes(unsigned char* dst, const unsi
     for (u32 i = n16 * 16u + threadIdx.x; i < bytes; i += blockDim.x) dst[i] = src[i];
 }
 
-static __device__ __forceinline__ table_ref stage_table(unsigned char* sm, const unsigned char* __restrict__ tab)
+// the table's sections: in global memory (large tables, L2 / L1 cached) or the staged
+// copy in shared memory
+static __device__ __forceinline__ table_ref table_at(unsigned char* sm, const unsigned char* __restrict__ tab)
 {
     table_ref t;
     t.gm = tab;
 #if FT_TABLE_GLOBAL
-    // large tables stay in global memory (L2 / L1 cached)
     (void)sm;
 #if FT_PREC == 0
     t.w = tab + T_W64;
@@ -2115,24 +2133,41 @@ static __device__ __forceinline__ table_ref stage_table(unsigned char* sm, const
     t.ri = tab + T_RI32;
 #endif
     t.meta = tab + T_META;
-    return t;
-#endif
-#if FT_PREC == 0
-    copy_bytes(sm, tab, 25u * T_ENTRIES);
+#elif FT_PREC == 0
     t.w = sm + T_W64;
     t.Jr = sm + T_JR64;
     t.ri = sm + T_RI64;
     t.meta = sm + T_META;
 #else
-    copy_bytes(sm, tab + T_F32, 16u * T_ENTRIES);
-    copy_bytes(sm + 16u * T_ENTRIES, tab + T_META, T_ENTRIES);
     t.w = sm;
     t.Jr = sm + 4u * T_ENTRIES;
     t.ri = sm + 8u * T_ENTRIES;
     t.meta = sm + 16u * T_ENTRIES;
 #endif
-    __syncthreads();
     return t;
+}
+
+// the block's copy of a staged table (no barrier)
+static __device__ __forceinline__ void copy_table(unsigned char* sm, const unsigned char* __restrict__ tab)
+{
+#if FT_TABLE_GLOBAL
+    (void)sm;
+    (void)tab;
+#elif FT_PREC == 0
+    copy_bytes(sm, tab, 25u * T_ENTRIES);
+#else
+    copy_bytes(sm, tab + T_F32, 16u * T_ENTRIES);
+    copy_bytes(sm + 16u * T_ENTRIES, tab + T_META, T_ENTRIES);
+#endif
+}
+
+static __device__ __forceinline__ table_ref stage_table(unsigned char* sm, const unsigned char* __restrict__ tab)
+{
+    copy_table(sm, tab);
+#if !FT_TABLE_GLOBAL
+    __syncthreads();
+#endif
+    return table_at(sm, tab);
 }
 
 // ------------------------------------------------------------------ per-thread accumulators
@@ -2140,7 +2175,9 @@ static __device__ __forceinline__ table_ref stage_table(unsigned char* sm, const
 // words), which keeps them out of the register budget of the sampling code:
 //   FP64 form: Neumaier-compensated FP64 sums per sample.
 //   mixed form: Kahan-compensated FP32 sums per sample, folded into the FP64
-//   Neumaier sums every 256 samples.
+//   Neumaier sums every 256 kept samples; the sample counters too (FP32 counts since
+//   the last fold, FP64 totals), so that no accumulator state is held in registers
+//   across the per-sample code.
 // Slots: 4 per eps order (re f, re f^2, im f, im f^2).
 #if FT_MODE == 0
 #define ACC_PARTS 2   // undeformed integrand: real parts only
@@ -2148,22 +2185,14 @@ static __device__ __forceinline__ table_ref stage_table(unsigned char* sm, const
 #define ACC_PARTS 4
 #endif
 #define ACC_NS (ACC_PARTS * FT_K)
-#if FT_PREC == 0
-#define ACC_BYTES_PER_THREAD (ACC_NS * 16)
-#else
-#define ACC_BYTES_PER_THREAD (ACC_NS * 24)
-#endif
 #define ACC_SMEM_OFFSET ((SM_USED + 15u) & ~15u)
+// mixed form, counters: kept, dropped, queued, exact
+#define ACC_NC 4
 
+#if FT_PREC == 0
 struct accum {
     double* S;   // [slot][thread] sums
     double* C;   // [slot][thread] Neumaier compensations
-#if FT_PREC == 1
-    float* Sf;   // [slot][thread] FP32 Kahan sums
-    float* Cf;
-    int since_fold;
-    float keptf, droppedf, queuedf, exactf;   // counters below 2^24 between folds
-#endif
     double kept, dropped, queued, exact, robust;
 
     __device__ __forceinline__ void init(unsigned char* smem_acc)
@@ -2171,20 +2200,10 @@ struct accum {
         const int t = threadIdx.x;
         S = (double*)smem_acc + t;
         C = S + ACC_NS * FT_BLOCK;
-#if FT_PREC == 1
-        Sf = (float*)((double*)smem_acc + 2 * ACC_NS * FT_BLOCK) + t;
-        Cf = Sf + ACC_NS * FT_BLOCK;
-        since_fold = 0;
-        keptf = droppedf = queuedf = exactf = 0.0f;
-#endif
 #pragma unroll
         for (int s = 0; s < ACC_NS; s++) {
             S[s * FT_BLOCK] = 0.0;
             C[s * FT_BLOCK] = 0.0;
-#if FT_PREC == 1
-            Sf[s * FT_BLOCK] = 0.0f;
-            Cf[s * FT_BLOCK] = 0.0f;
-#endif
         }
         kept = dropped = queued = exact = robust = 0.0;
     }
@@ -2212,56 +2231,9 @@ struct accum {
         }
     }
 
-#if FT_PREC == 1
-    __device__ __forceinline__ void add32(const cx<float>* R)
-    {
-        keptf += 1.0f;
-#pragma unroll
-        for (int j = 0; j < FT_K; j++) {
-            if (FT_ONLY_PSI && j > 0) break;
-            const float re = R[j].re, im = R[j].im;
-            const float v[4] = {re, re * re, im, im * im};
-#pragma unroll
-            for (int q = 0; q < ACC_PARTS; q++) {
-                const int o = (ACC_PARTS * j + q) * FT_BLOCK;
-                const float sf = Sf[o];
-                const float y = v[q] - Cf[o];
-                const float tt = sf + y;
-                Cf[o] = (tt - sf) - y;
-                Sf[o] = tt;
-            }
-        }
-        if (++since_fold == 256) fold();
-    }
-    __device__ __forceinline__ void note32(float d, float q, float e)
-    {
-        droppedf += d;
-        queuedf += q;
-        exactf += e;
-    }
-    __device__ __forceinline__ void fold()
-    {
-        since_fold = 0;
-#pragma unroll
-        for (int s = 0; s < ACC_NS; s++) {
-            nadd(s, (double)Sf[s * FT_BLOCK] - (double)Cf[s * FT_BLOCK]);
-            Sf[s * FT_BLOCK] = 0.0f;
-            Cf[s * FT_BLOCK] = 0.0f;
-        }
-        kept += keptf;
-        dropped += droppedf;
-        queued += queuedf;
-        exact += exactf;
-        keptf = droppedf = queuedf = exactf = 0.0f;
-    }
-#endif
-
     // block-wide: every thread of the block calls it; the block's sums go to dst[0 .. ACC_SLOTS)
     __device__ __forceinline__ void finish(double* dst)
     {
-#if FT_PREC == 1
-        fold();
-#endif
         double vals[ACC_SLOTS];
 #pragma unroll
         for (int s = 0; s < 8 * FT_K; s++) vals[s] = 0.0;
@@ -2284,6 +2256,120 @@ struct accum {
         block_reduce(vals, dst);
     }
 };
+#else
+// Shared-memory layout from ACC_SMEM_OFFSET, [slot][thread]: S, C (ACC_NS doubles
+// each), N (ACC_NC doubles), then Sf, Cf (ACC_NS floats each), Nf (ACC_NC floats).
+// Every address is the block's fixed offset plus the thread index, so the struct holds
+// nothing but the base.
+#define ACC_D(k) (((double*)base)[(k) * FT_BLOCK + threadIdx.x])
+#define ACC_F(k) (((float*)((double*)base + (2 * ACC_NS + ACC_NC) * FT_BLOCK))[(k) * FT_BLOCK + threadIdx.x])
+struct accum {
+    unsigned char* base;
+
+    __device__ __forceinline__ double& S(int s) { return ACC_D(s); }
+    __device__ __forceinline__ double& C(int s) { return ACC_D(ACC_NS + s); }
+    __device__ __forceinline__ double& N(int c) { return ACC_D(2 * ACC_NS + c); }
+    __device__ __forceinline__ float& Sf(int s) { return ACC_F(s); }
+    __device__ __forceinline__ float& Cf(int s) { return ACC_F(ACC_NS + s); }
+    __device__ __forceinline__ float& Nf(int c) { return ACC_F(2 * ACC_NS + c); }
+
+    __device__ __forceinline__ void init(unsigned char* smem_acc)
+    {
+        base = smem_acc;
+#pragma unroll
+        for (int s = 0; s < ACC_NS; s++) {
+            S(s) = 0.0;
+            C(s) = 0.0;
+            Sf(s) = 0.0f;
+            Cf(s) = 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < ACC_NC; c++) {
+            N(c) = 0.0;
+            Nf(c) = 0.0f;
+        }
+    }
+
+    __device__ __forceinline__ void nadd(int slot, double v)
+    {
+        const double s = S(slot);
+        const double t = s + v;
+        C(slot) += (fabs(s) >= fabs(v)) ? ((s - t) + v) : ((v - t) + s);
+        S(slot) = t;
+    }
+
+    __device__ __forceinline__ void add32(const cx<float>* R)
+    {
+#pragma unroll
+        for (int j = 0; j < FT_K; j++) {
+            if (FT_ONLY_PSI && j > 0) break;
+            const float re = R[j].re, im = R[j].im;
+            const float v[4] = {re, re * re, im, im * im};
+#pragma unroll
+            for (int q = 0; q < ACC_PARTS; q++) {
+                const int o = ACC_PARTS * j + q;
+                const float sf = Sf(o);
+                const float y = v[q] - Cf(o);
+                const float tt = sf + y;
+                Cf(o) = (tt - sf) - y;
+                Sf(o) = tt;
+            }
+        }
+        const float k = Nf(0) + 1.0f;
+        Nf(0) = k;
+        if (k == 256.0f) fold();
+    }
+    // every sample: dropped d, queued q (constants 0 or 1 at the call sites), exact steps e
+    __device__ __forceinline__ void note32(float d, float q, float e)
+    {
+        if (d != 0.0f) Nf(1) += d;
+        if (q != 0.0f) Nf(2) += q;
+        if (e != 0.0f) Nf(3) += e;
+    }
+    __device__ __forceinline__ void fold()
+    {
+#pragma unroll
+        for (int s = 0; s < ACC_NS; s++) {
+            nadd(s, (double)Sf(s) - (double)Cf(s));
+            Sf(s) = 0.0f;
+            Cf(s) = 0.0f;
+        }
+#pragma unroll
+        for (int c = 0; c < ACC_NC; c++) {
+            N(c) += (double)Nf(c);
+            Nf(c) = 0.0f;
+        }
+    }
+
+    // block-wide: every thread of the block calls it; the block's sums go to dst[0 .. ACC_SLOTS)
+    __device__ __forceinline__ void finish(double* dst)
+    {
+        fold();
+        double vals[ACC_SLOTS];
+#pragma unroll
+        for (int s = 0; s < 8 * FT_K; s++) vals[s] = 0.0;
+#pragma unroll
+        for (int s = 0; s < ACC_NS; s++) {
+            const double sv = S(s), cv = C(s);
+            const double h = sv + cv;
+            // slot s = (order j, part q) -> output pair 4 j + q
+            const int o = 4 * (s / ACC_PARTS) + (s % ACC_PARTS);
+            vals[2 * o] = h;
+            vals[2 * o + 1] = cv - (h - sv);
+        }
+        vals[ACC_KEPT] = N(0);
+        vals[ACC_DROPPED] = N(1);
+        vals[ACC_QUEUED] = N(2);
+        vals[ACC_EXACT] = N(3);
+        vals[ACC_ROBUST] = 0.0;
+#pragma unroll
+        for (int s = ACC_ROBUST + 1; s < ACC_SLOTS; s++) vals[s] = 0.0;
+        block_reduce(vals, dst);
+    }
+};
+#undef ACC_D
+#undef ACC_F
+#endif
 
 template <class T>
 static __device__ __forceinline__ void write_record(u64 i, const unsigned char* ord, const cx<T>* R, bool ok,
@@ -2333,11 +2419,11 @@ static __device__ __forceinline__ void sample64(xo& g, const table_ref& tr, cons
 // Samples [first, last) of the stream, g holding the state of sample `first`.  In the
 // mixed form, samples whose FP32 evaluation is not trustworthy are queued for the FP64
 // pass and left out of the sums here: 5 words, the sample (its index in the
-// single-integral kernels, `qtag | (i - first)` naming the work item in the batch
-// kernels) and its stream state.
+// single-integral kernels; item << BQ_ITEM_SHIFT | lane << BQ_LANE_SHIFT | (i - first)
+// naming the block's work item in the batch kernels) and its stream state.
 static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, const double* __restrict__ prm,
                                                     u64 first, u64 last, u64 chunk, accum& A, u64* __restrict__ queue,
-                                                    unsigned int* __restrict__ qcount, unsigned int qcap, u64 qtag,
+                                                    unsigned int* __restrict__ qcount, unsigned int qcap,
                                                     unsigned char* __restrict__ rec_order, double* __restrict__ rec_X,
                                                     double* __restrict__ rec_R, unsigned char* __restrict__ rec_flags)
 {
@@ -2345,7 +2431,6 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
     const float* pf = (const float*)(prm + P_SIZE);
     const float* pd = (const float*)(prm + P_SIZE + (P_SIZE + 1) / 2);   // two-float pairs
 #endif
-    (void)qtag;
     (void)chunk;
 #if FT_VARIANT & 4
     // Every thread of the block makes `chunk` trips and the block starts each sample
@@ -2381,7 +2466,7 @@ static __device__ __forceinline__ void sample_range(xo& g, const table_ref& tr, 
             if (slot < qcap) {
                 u64* q = queue + (size_t)slot * 5;
 #if FT_BATCH
-                q[0] = qtag | (i - first);
+                q[0] = (s_batch_item << BQ_ITEM_SHIFT) | ((u64)threadIdx.x << BQ_LANE_SHIFT) | (i - first);
 #else
                 q[0] = i;
 #endif
@@ -2431,7 +2516,7 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample(
 
     accum A;
     A.init(smem + ACC_SMEM_OFFSET);
-    sample_range(g, tr, prm, first, last, chunk, A, queue, qcount, qcap, 0, rec_order, rec_X, rec_R, rec_flags);
+    sample_range(g, tr, prm, first, last, chunk, A, queue, qcount, qcap, rec_order, rec_X, rec_R, rec_flags);
     A.finish(acc_out + (size_t)blockIdx.x * ACC_SLOTS);
 }
 
@@ -2487,13 +2572,6 @@ struct batch_inst {
     u64 pad[3];
 };
 
-// first word of an FP64-pass queue entry: item << 28 | lane << 18 | offset of the
-// sample in the lane's chunk (the other four hold the sample's stream state)
-#define BQ_ITEM_SHIFT 28
-#define BQ_LANE_SHIFT 18
-#define BQ_OFF_MASK ((1ull << BQ_LANE_SHIFT) - 1ull)
-#define BQ_LANE_MASK 1023ull
-
 // the instance owning `item`: the last instance whose first_item <= item
 static __device__ __forceinline__ int find_instance(const batch_inst* __restrict__ inst, int ninst, u64 item)
 {
@@ -2508,6 +2586,10 @@ static __device__ __forceinline__ int find_instance(const batch_inst* __restrict
     return lo;
 }
 
+// parameter block of the current instance, staged beside its table (P_SIZE doubles,
+// the same as floats, then as two-float pairs)
+#define PRM_WORDS (P_SIZE + (P_SIZE + 1) / 2 + P_SIZE)
+
 extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample_batch(
     const batch_inst* __restrict__ inst, int ninst, const u64* __restrict__ total_items,
     const u64* __restrict__ item_state, const u64* __restrict__ lanepw, int lanebits, u64 chunk,
@@ -2515,27 +2597,35 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample_batch(
     unsigned int* __restrict__ qcount, unsigned int qcap)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ u64 s_item;
+    // the instance's table and parameters sit at fixed shared-memory addresses, so the
+    // per-sample code holds no pointer to them in registers
+    __shared__ __align__(16) double s_prm[PRM_WORDS];
     __shared__ int s_inst;
-    const u64 total = *total_items;
     int cur = -1;
-    table_ref tr;
     for (;;) {
         if (threadIdx.x == 0) {
             const u64 it = atomicAdd(counter, 1ull);
-            s_item = it;
-            s_inst = it < total ? find_instance(inst, ninst, it) : -1;
+            s_batch_item = it;
+            s_inst = it < *total_items ? find_instance(inst, ninst, it) : -1;
         }
-        // also orders this item's table staging after every thread's previous item
+        // also orders this item's staging after every thread's previous item
         __syncthreads();
-        const u64 it = s_item;
         const int id = s_inst;
         if (id < 0) break;
         if (id != cur) {
-            tr = stage_table(smem, inst[id].tab);
+            copy_table(smem, inst[id].tab);
+            const double* __restrict__ src = inst[id].prm;
+            for (int k = threadIdx.x; k < PRM_WORDS; k += FT_BLOCK) s_prm[k] = src[k];
+            if (threadIdx.x == 0) s_batch_tab = inst[id].tab;
+            __syncthreads();
             cur = id;
         }
-        const double* prm = inst[id].prm;
+#if FT_TABLE_GLOBAL
+        const table_ref tr = table_at(smem, s_batch_tab);
+#else
+        const table_ref tr = table_at(smem, nullptr);
+#endif
+        const u64 it = s_batch_item;
         const u64 n = inst[id].nsamples;
         const u64 first = (it - inst[id].first_item) * (u64)FT_BLOCK * chunk + (u64)threadIdx.x * chunk;
         u64 last = first + chunk;
@@ -2544,9 +2634,11 @@ extern "C" __global__ void __launch_bounds__(FT_BLOCK, FT_MINB) ft_sample_batch(
         skip_lanes(g, threadIdx.x, lanepw, lanebits);
         accum A;
         A.init(smem + ACC_SMEM_OFFSET);
-        sample_range(g, tr, prm, first, last, chunk, A, queue, qcount, qcap,
-                     (it << BQ_ITEM_SHIFT) | ((u64)threadIdx.x << BQ_LANE_SHIFT), nullptr, nullptr, nullptr, nullptr);
-        A.finish(acc_out + it * ACC_SLOTS);
+        sample_range(g, tr, s_prm, first, last, chunk, A, queue, qcount, qcap, nullptr, nullptr, nullptr, nullptr);
+        // read before the reduction's barriers, after which the first thread may take
+        // the next item
+        double* dst = acc_out + s_batch_item * ACC_SLOTS;
+        A.finish(dst);
     }
 }
 
