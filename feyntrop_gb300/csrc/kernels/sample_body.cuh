@@ -1539,29 +1539,23 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
         }
     }
     auto Gx = [&](int i, int j) -> df { return (i == FT_V - 1 || j == FT_V - 1) ? df_mk(0.0f) : G[i][j]; };
-    // (G_pq + G_rs) - (G_pt + G_uv) over the terms without the ground vertex (its row of
-    // L^-1 is zero), so that no zero is added
-    auto gcomb = [&](int p1, int q1, int p2, int q2, int m1, int n1, int m2, int n2) -> df {
-        df acc = df_mk(0.0f);
-        bool any = false;
-        auto put = [&](int i, int j, bool neg) {
-            if (i == FT_V - 1 || j == FT_V - 1) return;
-            const df v = neg ? df_neg(G[i][j]) : G[i][j];
-            acc = any ? df_add(acc, v) : v;
-            any = true;
-        };
-        put(p1, q1, false);
-        put(p2, q2, false);
-        put(m1, n1, true);
-        put(m2, n2, true);
-        return acc;
-    };
     df kappa;
     kappa.hi = pd[2 * P_DEF];
     kappa.lo = pd[2 * P_DEF + 1];
 #pragma unroll
     for (int a2 = 0; a2 < FT_E; a2++) {
         const int ka = FT_EK[a2], la = FT_EL[a2];
+        // w = row a2 of (edge incidence) L^-1, w_v = G_{ka v} - G_{la v} (the ground's row of
+        // L^-1 is zero): edge a2's resistance combination with any edge (k, l),
+        // G_ka,k + G_la,l - G_ka,l - G_la,k, is then w_k - w_l.  The entries no edge
+        // pair reads are dropped at compile time.
+        df w[FT_N];
+#pragma unroll
+        for (int v = 0; v < FT_N; v++)
+            w[v] = ka == FT_V - 1 ? df_neg(G[la][v]) : (la == FT_V - 1 ? G[ka][v] : df_sub(G[ka][v], G[la][v]));
+        auto wd = [&](int k, int l) -> df {
+            return k == FT_V - 1 ? df_neg(w[l]) : (l == FT_V - 1 ? w[k] : df_sub(w[k], w[l]));
+        };
         df sig_hb[FT_RANK];
         df s = df_mk(0.0f);
 #pragma unroll
@@ -1572,7 +1566,7 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
             sig_hb[r] = df_mul(sg, hb[r][a2]);
             s = r == 0 ? df_mul(sig_hb[r], hb[r][a2]) : df_fma(sig_hb[r], hb[r][a2], s);
         }
-        const df t = gcomb(ka, ka, la, la, ka, la, ka, la);
+        const df t = wd(ka, la);
         // an edge whose ends float together: the FP64 pass takes the sample
         cancel |= ka != FT_V - 1 && !(df_f(t) > 1e-7f * (df_f(Gx(ka, ka)) + df_f(Gx(la, la))));
         const df xi = df_of(XiT[a2]);
@@ -1584,15 +1578,17 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
         theta_out[a2] = df_mul(df_sub(m2, xas), kappa);
         // 2 xa s (1/x - xa t)
         H_out[a2][a2] = 2.0f * df_f(df_mul(xas, df_sub(xi, df_mul(xa, t))));
+        // the off-diagonal entries are FP32 products of their (two-float) factors
+        const float xaf = df_f(xa);
 #pragma unroll
         for (int b = a2 + 1; b < FT_E; b++) {
             const int kb = FT_EK[b], lb = FT_EL[b];
             df s2 = df_mk(0.0f);
 #pragma unroll
             for (int r = 0; r < FT_RANK; r++) s2 = r == 0 ? df_mul(sig_hb[r], hb[r][b]) : df_fma(sig_hb[r], hb[r][b], s2);
-            const df t2 = gcomb(ka, kb, la, lb, ka, lb, la, kb);
+            const df t2 = wd(kb, lb);
             const float xb = Xi32[b];
-            H_out[a2][b] = -2.0f * df_f(df_mul(xa, df_mk(xb * xb))) * df_f(s2) * df_f(t2);
+            H_out[a2][b] = -2.0f * (xaf * (xb * xb)) * df_f(s2) * df_f(t2);
         }
     }
 }
