@@ -147,12 +147,14 @@ std::string class_id(const ft::kernel_key& k)
 std::vector<double> padded_params(const ft_plan& pl, int R)
 {
     const int E = pl.P.E, n = pl.P.V - 1, r0 = (int)pl.sigma.size();
-    std::vector<double> p(8 + 2 * E + R + (size_t)R * n, 0.0);
+    const size_t tail = pl.prm.size() - (8 + 2 * E + r0 + (size_t)r0 * n);   // P~'s external block
+    std::vector<double> p(8 + 2 * E + R + (size_t)R * n + tail, 0.0);
     std::copy(pl.prm.begin(), pl.prm.begin() + 8 + 2 * E, p.begin());
     for (int r = 0; r < r0; r++) {
         p[8 + 2 * E + r] = pl.sigma[r];
         for (int i = 0; i < n; i++) p[8 + 2 * E + R + (size_t)r * n + i] = pl.q[(size_t)r * n + i];
     }
+    std::copy(pl.prm.end() - tail, pl.prm.end(), p.end() - tail);
     return p;
 }
 

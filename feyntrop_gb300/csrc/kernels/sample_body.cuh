@@ -138,7 +138,8 @@ static __device__ constexpr bool first_in_slot(int e)
 
 // ------------------------------------------------------------------ parameter block
 // doubles: 0 D, 1 W, 2 IGtr, 3 def_ref, 4 1/(D/2*L+W), 5 Jr(full), 6 unused, 7 unused,
-// then m2[E], nu[E], sigma[RANK], q[RANK][N]
+// then m2[E], nu[E], sigma[RANK], q[RANK][N], then P~ on the external rows [Q0, N)
+// (its upper triangle row by row, off-diagonal entries doubled)
 #define P_D 0
 #define P_W 1
 #define P_IGTR 2
@@ -149,7 +150,11 @@ static __device__ constexpr bool first_in_slot(int e)
 #define P_NU (8 + FT_E)
 #define P_SIG (8 + 2 * FT_E)
 #define P_Q (8 + 2 * FT_E + FT_RANK)
-#define P_SIZE (8 + 2 * FT_E + FT_RANK + FT_RANK * FT_N)
+#define FT_NE (FT_N - FT_Q0)
+#define P_PT (8 + 2 * FT_E + FT_RANK + FT_RANK * FT_N)
+#define P_SIZE (P_PT + FT_NE * (FT_NE + 1) / 2)
+// entry (j, k), j <= k, of the external block of P~ (indices from Q0)
+#define PT_AT(j, k) (P_PT + (j) * FT_NE - (j) * ((j) - 1) / 2 + ((k) - (j)))
 // the same block as floats follows at prm + P_SIZE, then as two-float (hi, lo) pairs at
 // prm + P_SIZE + (P_SIZE + 1) / 2 (the mixed form reads only those two)
 
@@ -1336,15 +1341,16 @@ static __device__ FT_BIGFN cdf expi_df(df x)
 // Conductances y_e = e^(-i theta_e) / X_e from the two-float contour and sector point,
 // the conductance-form elimination of `elim`, the product of its pivots (rescaled by
 // powers of two as it goes: det L(y) = det * 2^det_e) and
-// V = -sum_r sigma_r q_r^T L(y)^-1 q_r + sum_e m2_e X_e e^(i theta_e).
+// V = -sum_jk P~_jk (L(y)^-1)_jk + sum_e m2_e X_e e^(i theta_e) (the reference's
+// -sum_r sigma_r q_r^T L^-1 q_r, contracted with P~ itself here).
 struct cblock {
     cdf V;
     cdf det;
     int det_e;
     bool ok;       // pivots and the determinant finite and non-zero
     float growth;  // smallest pivot-to-row-size ratio of the elimination
-    float mag;     // sum of the magnitudes of V's terms
-    float qmag;    // the same through the forward substitutions: sum_r |sigma_r| sum_i |y_i^2 / d_i| + masses
+    float mag;     // sum of the magnitudes of V's terms: masses, and one term per external row
+    float qmag;    // the same through the row quadratic forms: sum_i |1/d_i| sum_jk |P~_jk| |U_ij| |U_ik| + mag
 };
 static __device__ __forceinline__ float cmag_hi(const cdf& z) { return fabsf(z.re.hi) + fabsf(z.im.hi); }
 
@@ -1410,28 +1416,64 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
                 if (NZC(k, j)) c[i][j] = cdf_fma(a[k][i], c[k][j], c[i][j]);
         }
     }
+    // The momentum part, sum_jk P~_jk (L(y)^-1)_jk over the external rows [Q0, N) (P~
+    // vanishes elsewhere).  The forward substitution is y = U q with U unit lower
+    // triangular, U_ij = sum_{j <= k < i} a_ki U_kj, so L^-1 = U^T diag(1/d) U there and
+    // the part is sum_i (u_i^T P~ u_i) / d_i, u_i the i-th row of U: one quadratic form of
+    // P~ per row instead of one forward substitution per term of its low-rank split.
     float qmag = 0.0f;
+#if FT_NE > 0
+    {
+        auto ptd = [&](int j, int k) -> df { return pdf(PT_AT(j, k)); };
+        cdf U[FT_NE][FT_NE];   // U[i][j], j < i (indices from Q0)
+        cdf vq = cdf_zero();
 #pragma unroll
-    for (int r = 0; r < FT_RANK; r++) {
-        cdf yv[FT_N];
-        cdf sr = cdf_zero();
-        float qm = 0.0f;
+        for (int ii = 0; ii < FT_NE; ii++) {
+            const int i = FT_Q0 + ii;
 #pragma unroll
-        for (int i = FT_Q0; i < FT_N; i++) {
-            cdf yi = cdf_mk(pdf(P_Q + r * FT_N + i), df_mk(0.0f));
+            for (int jj = 0; jj < ii; jj++) {
+                const int j = FT_Q0 + jj;
+                cdf u = cdf_zero();
+                bool any = false;
+                if (NZC(j, i)) {
+                    u = a[j][i];
+                    any = true;
+                }
 #pragma unroll
-            for (int k = FT_Q0; k < i; k++)
-                if (NZC(k, i)) yi = cdf_fma(a[k][i], yv[k], yi);
-            yv[i] = yi;
-            const cdf t = (yi * yi) * dinv[i];
-            qm += cmag_hi(t);
-            sr = i == FT_Q0 ? t : sr + t;
+                for (int kk = jj + 1; kk < ii; kk++) {
+                    const int k = FT_Q0 + kk;
+                    if (!NZC(k, i)) continue;
+                    u = any ? cdf_fma(a[k][i], U[kk][jj], u) : a[k][i] * U[kk][jj];
+                    any = true;
+                }
+                U[ii][jj] = u;
+            }
+            // Q = u^T P~ u with u = (U_i0 .. U_i,i-1, 1): Q = P_ii + sum_j u_j w_j,
+            // w_j = sum_{j <= k < i} P_jk u_k + P_ji (off-diagonal P doubled)
+            cdf Q = cdf_mk(ptd(ii, ii), df_mk(0.0f));
+            float qm = fabsf(ptd(ii, ii).hi);
+#pragma unroll
+            for (int jj = 0; jj < ii; jj++) {
+                cdf w = ptd(jj, jj) * U[ii][jj];
+                float wm = fabsf(ptd(jj, jj).hi) * cmag_hi(U[ii][jj]);
+#pragma unroll
+                for (int kk = jj + 1; kk < ii; kk++) {
+                    w = w + ptd(jj, kk) * U[ii][kk];
+                    wm += fabsf(ptd(jj, kk).hi) * cmag_hi(U[ii][kk]);
+                }
+                w.re = df_add(w.re, ptd(jj, ii));
+                wm += fabsf(ptd(jj, ii).hi);
+                Q = cdf_fma(U[ii][jj], w, Q);
+                qm += cmag_hi(U[ii][jj]) * wm;
+            }
+            const cdf t = Q * dinv[i];
+            vq = ii == 0 ? t : vq + t;
+            mag += cmag_hi(t);
+            qmag += qm * cmag_hi(dinv[i]);
         }
-        const df sg = pdf(P_SIG + r);
-        v = v - sg * sr;
-        mag += fabsf(sg.hi) * cmag_hi(sr);
-        qmag += fabsf(sg.hi) * qm;
+        v = v - vq;
     }
+#endif
     o.V = v;
     o.det = det;
     o.det_e = det_e;

@@ -203,8 +203,8 @@ namespace {
 void build_blocks(ft_plan& pl)
 {
     const ft::prepared& p = pl.P;
-    const int E = p.E, n = p.V - 1, R = (int)pl.sigma.size();
-    pl.prm.assign(8 + 2 * E + R + R * n, 0.0);
+    const int E = p.E, n = p.V - 1, R = (int)pl.sigma.size(), ne = n - pl.q0;
+    pl.prm.assign(8 + 2 * E + R + R * n + ne * (ne + 1) / 2, 0.0);
     pl.prm[0] = p.D;
     pl.prm[1] = p.W;
     pl.prm[2] = p.IGtr;
@@ -219,6 +219,10 @@ void build_blocks(ft_plan& pl)
         pl.prm[8 + 2 * E + r] = pl.sigma[r];
         for (int i = 0; i < n; i++) pl.prm[8 + 2 * E + R + r * n + i] = pl.q[r * n + i];
     }
+    // P~ on the external rows [q0, n): upper triangle row by row, off-diagonal doubled
+    // (the mixed form's deformed integrand contracts it with L(y)^-1 directly)
+    for (int j = 0, o = 8 + 2 * E + R + R * n; j < ne; j++)
+        for (int k = j; k < ne; k++) pl.prm[o++] = (j == k ? 1.0 : 2.0) * pl.kP[(size_t)(pl.q0 + j) * p.V + pl.q0 + k];
     const size_t N = 1ULL << E;
     const size_t f32 = (25 * N + 15) & ~(size_t)15;
     pl.tab.assign(f32 + 16 * N, 0);
