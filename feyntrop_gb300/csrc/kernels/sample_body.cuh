@@ -1343,12 +1343,27 @@ static __device__ FT_BIGFN cdf expi_df(df x)
 // powers of two as it goes: det L(y) = det * 2^det_e) and
 // V = -sum_jk P~_jk (L(y)^-1)_jk + sum_e m2_e X_e e^(i theta_e) (the reference's
 // -sum_r sigma_r q_r^T L^-1 q_r, contracted with P~ itself here).
+// deformed integrand, the two-float complex block (det L(y) and V): smallest accepted
+// pivot-to-row ratio, smallest |V| relative to the sum of its terms' magnitudes, and
+// largest W qmag / |V| (qmag: the magnitudes of every term summed into V, through the
+// row quadratic forms).  Two-float arithmetic keeps ~1e-14 of these magnitudes and
+// the sector point and contour it starts from ~1e-12, so the bounds only catch samples
+// whose cancellation would amplify that to ~1e-7.
+#ifndef ACC_GROWTH
+#define ACC_GROWTH 1e-5f
+#endif
+#ifndef ACC_V_CANCEL
+#define ACC_V_CANCEL 1e-6f
+#endif
+#ifndef ACC_V_AMPLIFY
+#define ACC_V_AMPLIFY 1e5f
+#endif
 struct cblock {
     cdf V;
     cdf det;
     int det_e;
     bool ok;       // pivots and the determinant finite and non-zero
-    float growth;  // smallest pivot-to-row-size ratio of the elimination
+    bool growth_ok;  // every pivot above ACC_GROWTH of its row's size
     float mag;     // sum of the magnitudes of V's terms: masses, and one term per external row
     float qmag;    // the same through the row quadratic forms: sum_i |1/d_i| sum_jk |P~_jk| |U_ij| |U_ik| + mag
 };
@@ -1389,7 +1404,7 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
     cdf det = cdf_mk(df_mk(1.0f), df_mk(0.0f));
     int det_e = 0;
     bool ok = true;
-    float worst = 1.0f;
+    bool growth_ok = true;
 #pragma unroll
     for (int k = 0; k < FT_N; k++) {
         cdf dk = g[k];
@@ -1400,7 +1415,7 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
             dk = dk + c[k][j];
             row += cmag_hi(c[k][j]);
         }
-        worst = fminf(worst, cmag_hi(dk) / row);
+        growth_ok &= cmag_hi(dk) > ACC_GROWTH * row;
         det = det * dk;
         ok &= cdf_renorm(det, det_e);
         dinv[k] = cdf_inv(dk);
@@ -1478,7 +1493,7 @@ static __device__ __forceinline__ void complex_block(const df* theta, const f2* 
     o.det = det;
     o.det_e = det_e;
     o.ok = ok;
-    o.growth = worst;
+    o.growth_ok = growth_ok;
     o.mag = mag;
     o.qmag = qmag + mag;
 }
@@ -1691,21 +1706,6 @@ static __device__ __forceinline__ f2 f2_neg(f2 a) { return f2_make(-a.hi, -a.lo)
 #ifndef PIVOT_GROWTH
 #define PIVOT_GROWTH 0.02f
 #endif
-// deformed integrand, the two-float complex block (det L(y) and V): smallest accepted
-// pivot-to-row ratio, smallest |V| relative to the sum of its terms' magnitudes, and
-// largest W qmag / |V| (qmag: the magnitudes of every term summed into V, through the
-// forward substitutions).  Two-float arithmetic keeps ~1e-14 of these magnitudes and
-// the sector point and contour it starts from ~1e-12, so the bounds only catch samples
-// whose cancellation would amplify that to ~1e-7.
-#ifndef ACC_GROWTH
-#define ACC_GROWTH 1e-5f
-#endif
-#ifndef ACC_V_CANCEL
-#define ACC_V_CANCEL 1e-6f
-#endif
-#ifndef ACC_V_AMPLIFY
-#define ACC_V_AMPLIFY 1e5f
-#endif
 #define RLN2_HI 1.44269502162933349609375f
 #define RLN2_LO 1.925963033500011e-8f
 #define LN2_F 0.69314718055994531f
@@ -1884,8 +1884,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     // block, so that H is no longer live there.
     cx<float> pj = cmk(1.0f, 0.0f);
     int pj_e = 0;
-    float jgrowth = 1.0f;
-    bool jok = true;
+    bool jok = true;   // pivots above PIVOT_GROWTH of their rows, scaled product finite
     {
         cx<float> J[FT_E][FT_E];
         float sx[FT_E];
@@ -1902,7 +1901,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
             float row = m;
 #pragma unroll
             for (int j = k + 1; j < FT_E; j++) row += fabsf(J[k][j].re) + fabsf(J[k][j].im);
-            jgrowth = fminf(jgrowth, m / row);
+            jok &= m > PIVOT_GROWTH * row;
             pj = pj * piv;
             {
                 const float mx = fmaxf(fabsf(pj.re), fabsf(pj.im));
@@ -1922,8 +1921,7 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
             }
         }
     }
-    FT_DBG(29, jgrowth);
-    if (!jok || !(jgrowth > PIVOT_GROWTH)) {
+    if (!jok) {
         need64 = true;
         return false;
     }
@@ -1937,9 +1935,8 @@ static __device__ __forceinline__ bool integrand32(const float* pd, const float*
     }
     cblock cb;
     complex_block(theta, Xi2, pd, cb);
-    FT_DBG(27, cb.growth);
     // two-float pivots lose ~1e-14 / growth
-    if (!cb.ok || !(cb.growth > ACC_GROWTH)) {
+    if (!cb.ok || !cb.growth_ok) {
         need64 = true;
         return false;
     }
