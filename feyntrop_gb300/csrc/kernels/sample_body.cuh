@@ -1560,16 +1560,23 @@ static __device__ __forceinline__ void derivatives_df(const float* Xi32, const f
             Nm[i][j] = s;
         }
     }
+    // Nd[j][k] = N[j][k] / d_k, so that each term of G is one two-float multiply-add
+    df Nd[FT_N][FT_N];
+#pragma unroll
+    for (int j = 0; j < FT_N; j++)
+#pragma unroll
+        for (int k = j + 1; k < FT_N; k++)
+            if (NZM(j, k)) Nd[j][k] = df_mul(Nm[j][k], id[k]);
     df G[FT_N][FT_N];
 #pragma unroll
     for (int i = 0; i < FT_N; i++)
 #pragma unroll
         for (int j = i; j < FT_N; j++) {
             // k = j term has N[j][j] = 1
-            df s = (i == j) ? id[j] : (NZM(i, j) ? df_mul(Nm[i][j], id[j]) : df_mk(0.0f));
+            df s = (i == j) ? id[j] : (NZM(i, j) ? Nd[i][j] : df_mk(0.0f));
 #pragma unroll
             for (int k = j + 1; k < FT_N; k++)
-                if (NZM(i, k) && NZM(j, k)) s = df_fma(df_mul(Nm[i][k], Nm[j][k]), id[k], s);
+                if (NZM(i, k) && NZM(j, k)) s = df_fma(Nm[i][k], Nd[j][k], s);
             G[i][j] = s;
             G[j][i] = s;
         }
@@ -1754,12 +1761,13 @@ static __device__ FT_BIGFN f2 arg_f2(float x, float y, float xl, float yl)
     const float ax = fabsf(x), ay = fabsf(y);
     const bool sw = ay > ax;
     const float num = sw ? ax : ay, den = sw ? ay : ax;
-    const float a = den > 0.0f ? m_atan(num / den) : 0.0f;
+    // the ratio through the correctly rounded reciprocal (within 1.5 ulp of num / den)
+    const float a = den > 0.0f ? m_atan(num * rcp_(den)) : 0.0f;
     f2 r = sw ? f2_add(f2_make(PIO2_HI, PIO2_LO), -a) : f2_make(a, 0.0f);
     if (x < 0.0f) r = f2_add2(f2_make(2.0f * PIO2_HI, 2.0f * PIO2_LO), f2_neg(r));
     if (y < 0.0f) r = f2_neg(r);
     const float n2 = fmaf(x, x, y * y);
-    return n2 > 0.0f ? f2_add(r, (x * yl - y * xl) / n2) : r;
+    return n2 > 0.0f ? f2_add(r, (x * yl - y * xl) * rcp_(n2)) : r;
 }
 
 // Sets need64 when the FP32 / two-float evaluation cannot be trusted (the sample then
