@@ -895,17 +895,19 @@ static __device__ __forceinline__ int draw_sector32(xo& g, const table_ref& t, c
         float T = 0.0f;
         int e = 0, sure = -1;
         bool unsure = false;
-#pragma unroll
-        for (int c = 0; c < FT_E; c++) {
-            if (((sub >> c) & 1u) && sure < 0) {
-                T += w[sub ^ (1u << c)];
-                e = c;
-                const float d = T - Rf;
-                if (d > margin)
-                    sure = c;
-                else if (d >= -margin)
-                    unsure = true;
+        // the edges of the current subgraph in ascending order (its set bits), up to the
+        // first sure decision: the same comparisons as a scan over all E edges, without
+        // the trips over edges already cut
+        for (u32 left = sub; left != 0u; left &= left - 1u) {
+            const int c = __ffs(left) - 1;
+            T += w[sub ^ (1u << c)];
+            e = c;
+            const float d = T - Rf;
+            if (d > margin) {
+                sure = c;
+                break;
             }
+            if (d >= -margin) unsure = true;
         }
         int cut = sure >= 0 ? sure : e;
         if (unsure) {
