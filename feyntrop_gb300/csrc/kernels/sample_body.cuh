@@ -688,14 +688,12 @@ static __device__ __forceinline__ void draw_sector64(xo& g, const table_ref& t, 
         const double R = u01(g.next()) * JJr;
         double T = 0.0;
         int e = 0;
-        bool found = false;
-#pragma unroll
-        for (int c = 0; c < FT_E; c++) {
-            if (((sub >> c) & 1u) && !found) {
-                T += w[sub ^ (1u << c)];
-                e = c;
-                found = T > R;
-            }
+        // the subgraph's edges in ascending order (its set bits) until the running sum
+        // passes R, else the last one
+        for (u32 left = sub; left != 0u; left &= left - 1u) {
+            e = __ffs(left) - 1;
+            T += w[sub ^ (1u << e)];
+            if (T > R) break;
         }
         sub ^= 1u << e;
         JJr = Jr[sub];
