@@ -33,7 +33,9 @@
 //    of positive conductances and updates add positive products, so psi = det L *
 //    prod X has full relative accuracy whatever the spread of X.
 //  * phi/psi = -tr(L^-1 P~) with P~ = sum_r sigma_r q_r q_r^T (host eigen-split):
-//    each term is a forward substitution with the elimination multipliers.
+//    each term is a forward substitution with the elimination multipliers.  The
+//    mixed form's complex block instead contracts P~'s external block with L(y)^-1
+//    directly, one quadratic form of P~ per row of the substitution's triangular map.
 //  * Deformed branch: L^-1 from the positive factors, x-derivatives of phi/psi
 //    (srcs/laplacian.hpp:102-215), the complex Laplacian eliminated in the same
 //    conductance form with a pivot-growth check (the FP64 form's failing samples take
