@@ -13,6 +13,9 @@ import oracle_lib as ol
 pytestmark = pytest.mark.gpu
 
 PINS = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_pins.json")))
+# 50-digit values of the samples where the oracle's FP64 arithmetic is not exact
+# (tests/golden/make_six_point_truth.py)
+SIX_POINT_TRUTH = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "six_point_truth.json")))
 
 
 def grid(a, b):
@@ -51,6 +54,64 @@ def test_seventeen_edge_graph_matches_the_oracle():
     b = p.integrate(200_000, seed=1, precision=ft.MIXED)
     for j in range(2):
         assert abs(a["integral"][j][0][0] - b["integral"][j][0][0]) <= 1e-3 * a["integral"][j][0][1]
+    p.close()
+
+
+def six_point(graph, seed):
+    """Minkowski kinematics with momentum on all six vertices of `graph` (five external
+    rows of the reduced Laplacian): random scalar products, masses U[0.5, 2], lambda 0.5,
+    D = 6, 2 eps orders (the same inputs as tests/golden/make_six_point_truth.py)."""
+    import random
+    from feyntrop_gb300.workloads import kinematic_matrix
+    rng = random.Random(seed)
+    sp = {(i, j): (rng.uniform(0.5, 3) if i == j else rng.uniform(-5, 5)) for i in range(5) for j in range(i, 5)}
+    return {"graph": graph, "dimension": 6, "scalarproducts": kinematic_matrix(6, sp),
+            "masses_sqr": [rng.uniform(0.5, 2) for _ in graph], "num_eps_terms": 2, "lambda": 0.5, "N": 1000,
+            "seed": 0}
+
+
+@pytest.mark.parametrize("name", ["hexagon", "six_point_double_box"])
+def test_deformed_six_point_graphs_match_the_oracle(name):
+    """Deformed integrands whose momentum part spans five external rows: the one-loop
+    hexagon and the planar double box with momentum on every vertex.  Per sample
+    against the oracle (FP64 form 1e-9, mixed form 1e-5, its FP64 hand-offs 1e-9),
+    except the samples where the oracle's own FP64 value is off the 50-digit one by
+    more than 1e-11: there both forms are compared with the 50-digit value, within
+    their bound or ten times the oracle's own error there, whichever is larger (one
+    six-point double-box sample is conditioned so badly that any FP64 evaluation
+    misses it by ~3e-3: the oracle by 2.6e-3, the GPU's FP64 form by 3.3e-3)."""
+    if name == "hexagon":
+        graph = [[[i, (i + 1) % 6], 1] for i in range(6)]
+    else:
+        graph = [[[0, 1], 1], [[1, 2], 1], [[2, 3], 1], [[3, 4], 1], [[4, 5], 1], [[5, 0], 1], [[1, 4], 1]]
+    inp = six_point(graph, 11)
+    p = ft.Plan(inp)
+    assert p.info["deformed"]
+    n = SIX_POINT_TRUTH["n_samples"]
+    ref = ol.Prepared(inp).samples(0, 0, n)
+    # (in those sectors the oracle's value also depends on the host compiler's rounding)
+    R = ref["R"].copy()
+    floor = np.zeros(n)
+    for r in SIX_POINT_TRUTH["cases"][name]:
+        R[r["index"]] = np.array([complex(*z) for z in r["truth"]])
+        floor[r["index"]] = 10 * r["oracle_error"]
+    for prec, tol in ((ft.FP64, 1e-9), (ft.MIXED, 1e-5)):
+        rec = p.records(n, seed=0, precision=prec)
+        assert (rec["order"] == ref["order"]).all()
+        ok = ~ref["dropped"]
+        scale = np.abs(R[ok]).max(axis=1)
+        err = np.abs(rec["R"][ok] - R[ok]).max(axis=1) / scale
+        queued = (rec["flags"][ok] & 2) != 0
+        bound = np.maximum(np.where(queued, 1e-9, tol), floor[ok])
+        bad = np.nonzero(err > bound)[0]
+        assert bad.size == 0, (prec, [(int(np.nonzero(ok)[0][i]), float(err[i])) for i in bad[:5]])
+    a = p.integrate(400_000, seed=1, precision=ft.FP64)
+    b = p.integrate(400_000, seed=1, precision=ft.MIXED)
+    for j in range(2):
+        for part in range(2):
+            x, dx = a["integral"][j][part]
+            y, dy = b["integral"][j][part]
+            assert abs(x - y) <= 0.01 * dx + 1e-12, (j, part, x, y, dx)
     p.close()
 
 
