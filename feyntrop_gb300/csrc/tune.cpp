@@ -106,13 +106,30 @@ launch_shape default_shape(const kernel_key& k)
     return s;
 }
 
+// Shared memory of one block: the dynamic part (staged table, per-thread sums) plus the
+// kernel body's static arrays, the block reduction's per-warp slots and, in the batch
+// kernels, the staged parameter block (its doubles, floats and two-float pairs) and the
+// work-item variables.
+static unsigned block_smem_bytes(const kernel_key& k)
+{
+    const unsigned slots = 8u * (unsigned)k.K + 8u;
+    const unsigned red = (unsigned)(k.block / 32) * slots * 8u;
+    unsigned prm = 0;
+    if (k.batch) {
+        const unsigned n = (unsigned)(k.V - 1), ne = n - (unsigned)k.q0, r = (unsigned)k.rank;
+        const unsigned p = 8u + 2u * (unsigned)k.E + r + r * n + ne * (ne + 1u) / 2u;
+        prm = (p + (p + 1u) / 2u + p) * 8u + 64u;
+    }
+    return table_smem_bytes(k) + red + prm;
+}
+
 void apply_shape(kernel_key& k, const launch_shape& s)
 {
     k.block = s.block;
     k.minb = s.minb;
     k.variant = s.variant;
     // keep the warps per SM while halving the block until the shared memory fits
-    while (k.block > 64 && table_smem_bytes(k) > kSmemLimit) {
+    while (k.block > 64 && block_smem_bytes(k) > kSmemLimit) {
         k.block /= 2;
         k.minb = k.minb * 2 > 32 ? 32 : k.minb * 2;
     }
