@@ -93,3 +93,32 @@ def test_skip_matches_stepping():
     t = p.samples(11, 37, 3)
     assert (s["order"][37:] == t["order"]).all()
     assert (s["X"][37:] == t["X"]).all()
+
+
+def test_six_point_truth_fixture():
+    """tests/golden/six_point_truth.json (the 50-digit referee of the deformed six-point
+    GPU tests): its samples are this oracle's, and re-evaluating a few of them at 50
+    digits gives the recorded values."""
+    mp = pytest.importorskip("mpmath")
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+    import hp_truth
+    import make_six_point_truth as mk
+    fx = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "six_point_truth.json")))
+    for name, rows in fx["cases"].items():
+        inp = mk.six_point_input(mk.GRAPHS[name], 11)
+        prep = ol.Prepared(inp)
+        s = prep.samples(fx["seed"], 0, fx["n_samples"])
+        info = {"W": prep.W, "IGtr": prep.IGtr, "loops": prep.loops, "lambda_used": mk.LAMBDA, "deformed": True}
+        assert rows, name
+        worst = max(rows, key=lambda r: r["oracle_error"])
+        for r in rows:
+            i = r["index"]
+            t = np.array([complex(*z) for z in r["truth"]])
+            o = np.array([complex(*z) for z in r["oracle"]])
+            # the oracle's value in these sectors depends on the host compiler's rounding
+            assert np.abs(s["R"][i] - o).max() <= 1e-6 * np.abs(t).max()
+        for r in (rows[0], worst):
+            i = r["index"]
+            t = np.array(hp_truth.truth(inp, info, s["X"][i], s["psi_tr"][i], s["xi_tr"][i]))
+            assert np.abs(t - np.array([complex(*z) for z in r["truth"]])).max() <= 1e-14 * np.abs(t).max()
